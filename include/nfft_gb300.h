@@ -1,0 +1,58 @@
+/*
+ * nfft_gb300.h -- GB300-specific extensions of the NFFT C API.
+ *
+ * These entry points have no counterpart in the reference NFFT; they expose
+ * what a GPU caller needs beyond the host-array semantics of nfft3.h:
+ * device-resident operands (inputs already in HBM), the CUDA stream a plan
+ * runs on, per-stage timings, and the library's error state.  All take plain
+ * pointers and sizes; CUDA handles are passed as void*.
+ *
+ * Each function exists for both precisions: nfft_gb_* (double plans) and
+ * nfftf_gb_* (float plans).
+ */
+#ifndef NFFT_GB300_H
+#define NFFT_GB300_H
+
+#include "nfft3.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NFFTGB_DEFINE_API(X) \
+/* Run the plan on this cudaStream_t (NULL = the plan's own stream). */ \
+int X(gb_set_stream)(X(plan) *ths, void *cuda_stream); \
+void *X(gb_get_stream)(X(plan) *ths); \
+/* Device buffers of the plan: f_hat (N_total complex), f (M_total complex), \
+ * in the caller's natural orders, and x (M_total*d reals, node-major). */ \
+void *X(gb_device_f_hat)(X(plan) *ths); \
+void *X(gb_device_f)(X(plan) *ths); \
+void *X(gb_device_x)(X(plan) *ths); \
+/* Node set-up from a device copy of x (already in gb_device_x). */ \
+void X(gb_precompute_device)(X(plan) *ths); \
+/* Transforms on the device buffers, enqueued on the plan's stream; they do \
+ * not synchronise and do not touch the host arrays. */ \
+void X(gb_trafo_device)(X(plan) *ths); \
+void X(gb_adjoint_device)(X(plan) *ths); \
+/* Milliseconds of the last host-API transform per stage: \
+ * [0] D or D^T, [1] FFT, [2] B or B^T, [3] host<->device copies. */ \
+void X(gb_stage_times)(X(plan) *ths, float *ms4); \
+/* Kernel launches of the last transform (library kernels, not cuFFT). */ \
+int X(gb_last_launch_count)(X(plan) *ths);
+
+NFFTGB_DEFINE_API(NFFT_MANGLE_DOUBLE)
+NFFTGB_DEFINE_API(NFFT_MANGLE_FLOAT)
+
+/* Last error message recorded by the library (empty string if none).  Fatal
+ * errors also go through nfft_die / nfft_die_hook like the reference. */
+const char *nfft_gb_last_error(void);
+void nfft_gb_clear_error(void);
+
+/* 1 when the library was built for and runs on an sm_103 device. */
+int nfft_gb_device_ok(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NFFT_GB300_H */

@@ -1,0 +1,159 @@
+// gb_common.cuh -- shared types and device helpers of the GB300 NFFT library.
+//
+// Conventions (matching the reference NFFT 3):
+//  * x is node-major, x[j*d + t] in [-1/2, 1/2) (reference nfft.c:6185-6191);
+//  * f_hat is row-major over k_t = -N_t/2 .. N_t/2-1, last dimension fastest;
+//  * the oversampled grid g has n_t points per dimension in FFT order;
+//  * node j's window covers grid indices u_t .. u_t + 2m + 1 (mod n_t) with
+//    u_t = floor(x_t n_t) - m (reference nfft.c:324-340), and the window
+//    argument uses the unwrapped index (reference nfft.c:5838-5840).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#define GB_MAXD 8          // largest dimension d the library accepts
+#define GB_MAXW 66         // largest window width 2m+2 (m <= 32)
+
+namespace gb {
+
+template <typename R> struct Cx;
+template <> struct Cx<float> { typedef float2 T; };
+template <> struct Cx<double> { typedef double2 T; };
+
+// ---------------------------------------------------------------- errors
+void record_error(const char *fmt, ...);
+void fatal(const char *fmt, ...);  // records, then calls nfft_die (exits)
+void check_cuda(cudaError_t e, const char *what, const char *file, int line);
+void check_launch(const char *what, const char *file, int line);
+
+#define GB_CUDA(call) ::gb::check_cuda((call), #call, __FILE__, __LINE__)
+#define GB_LAUNCHED(name) ::gb::check_launch(name, __FILE__, __LINE__)
+
+// ---------------------------------------------------------------- geometry
+// Everything a transform kernel needs about the plan, passed by value.
+template <typename R>
+struct Geom {
+  int d;
+  int m;
+  int w;                 // 2m+2
+  int n[GB_MAXD];        // grid lengths
+  int N[GB_MAXD];        // bandwidths
+  R nR[GB_MAXD];         // (R) n_t
+  R b[GB_MAXD];          // KB shape parameter per dim, pi (2 - 1/sigma_t)
+  R mm;                  // (R) m * (R) m
+  long long M;           // nodes
+  long long n_total;
+  long long N_total;
+  // tiling of the grid for the shared-memory kernels
+  int T[GB_MAXD];        // tile edge per dim
+  int ntile[GB_MAXD];    // tiles per dim (n_t / T_t, rounded up)
+  int ext[GB_MAXD];      // padded subgrid edge T_t + w - 1
+};
+
+struct WorkItem {
+  int tile;    // linear tile id (row-major over ntile)
+  int start;   // first sorted node
+  int end;     // one past last sorted node
+  int pad;
+};
+
+#ifdef __CUDACC__
+// ---------------------------------------------------------------- window
+template <typename R> __device__ __forceinline__ R gb_pi();
+template <> __device__ __forceinline__ float gb_pi<float>() { return 3.14159265358979323846f; }
+template <> __device__ __forceinline__ double gb_pi<double>() { return 3.14159265358979323846; }
+
+__device__ __forceinline__ float gb_sqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double gb_sqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float gb_sinh(float v) { return sinhf(v); }
+__device__ __forceinline__ double gb_sinh(double v) { return sinh(v); }
+__device__ __forceinline__ float gb_sin(float v) { return sinf(v); }
+__device__ __forceinline__ double gb_sin(double v) { return sin(v); }
+__device__ __forceinline__ float gb_floor(float v) { return floorf(v); }
+__device__ __forceinline__ double gb_floor(double v) { return floor(v); }
+
+// Kaiser-Bessel window phi(xl) for grid length n, where xl = x - l/n
+// (reference include/infft.h:209-215): sinh(b s)/(pi s) with
+// s = sqrt(m^2 - (n xl)^2) inside the support, sin(b s)/(pi s) with
+// s = sqrt((n xl)^2 - m^2) outside, b/pi on the boundary.
+template <typename R>
+__device__ __forceinline__ R kb_phi(R xl, R nR, R mm, R b)
+{
+  const R t = xl * nR;
+  const R t2 = t * t;
+  const R arg = mm - t2;
+  if (arg > R(0)) {
+    const R s = gb_sqrt(arg);
+    return gb_sinh(b * s) / (gb_pi<R>() * s);
+  } else if (arg < R(0)) {
+    const R s = gb_sqrt(t2 - mm);
+    return gb_sin(b * s) / (gb_pi<R>() * s);
+  }
+  return b / gb_pi<R>();
+}
+
+// Unwrapped window start u = floor(x n) - m (reference nfft.c:324-332).  The
+// same expression is used by the binning and by every transform kernel so a
+// node lands in the same tile everywhere.
+template <typename R>
+__device__ __forceinline__ int node_u(R x, R nR, int m)
+{
+  return (int)gb_floor(x * nR) - m;
+}
+
+__device__ __forceinline__ int wrap(int i, int n)
+{
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+// window values of one node in one dimension: out[l] = phi(x - (u+l)/n)
+template <typename R, int W>
+__device__ __forceinline__ void node_psi(R x, int u, R nR, R mm, R b, R *out)
+{
+#pragma unroll
+  for (int l = 0; l < W; ++l)
+    out[l] = kb_phi<R>(x - R(u + l) / nR, nR, mm, b);
+}
+
+template <typename R>
+__device__ __forceinline__ void node_psi_rt(R x, int u, int w, R nR, R mm, R b, R *out)
+{
+  for (int l = 0; l < w; ++l)
+    out[l] = kb_phi<R>(x - R(u + l) / nR, nR, mm, b);
+}
+
+// complex helpers
+__device__ __forceinline__ float2 cmake(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 cmake(double a, double b) { return make_double2(a, b); }
+
+__device__ __forceinline__ void atomic_add_c(float2 *p, float2 v)
+{
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+__device__ __forceinline__ void atomic_add_c(double2 *p, double2 v)
+{
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+// global complex accumulate: one vector reduction for float2 on sm_90+
+__device__ __forceinline__ void global_add_c(float2 *p, float2 v)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  atomicAdd(p, v);
+#else
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+#endif
+}
+__device__ __forceinline__ void global_add_c(double2 *p, double2 v)
+{
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+#endif  // __CUDACC__
+
+}  // namespace gb

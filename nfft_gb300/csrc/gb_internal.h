@@ -1,0 +1,83 @@
+// gb_internal.h -- host-side interfaces between the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+// ---------------------------------------------------------------- scans/sort
+size_t scan_temp_bytes(size_t n);
+// out[i] = sum_{k<i} in[k]; out may not alias in.  total (device, nullable)
+// receives the sum of all n values.
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *total,
+                        void *temp, cudaStream_t s);
+
+size_t radix_temp_bytes(size_t n);
+// Stable LSD radix sort of (keys, vals) by the low key_bits bits of keys.
+// keys2/vals2 are n-element ping-pong buffers.  The sorted result ends in
+// keys/vals.
+void radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2,
+                      size_t n, int key_bits, void *temp, cudaStream_t s);
+
+// node binning
+template <typename R>
+void launch_node_keys(const R *x, const Geom<R> &g, uint32_t *tile_key, uint32_t *ref_key,
+                      uint32_t *idx, cudaStream_t s);
+template <typename R>
+void launch_gather_x(const R *x, const uint32_t *perm, R *xs, const Geom<R> &g, cudaStream_t s);
+void launch_tile_starts(const uint32_t *sorted_keys, long long M, int ntiles, uint32_t *start,
+                        cudaStream_t s);
+// fills items (capacity >= ntiles + M/chunk + 1); returns the item count
+// (synchronises the stream once)
+int build_work_items(const uint32_t *start, int ntiles, int chunk, WorkItem *items,
+                     uint32_t *cnt_tmp, uint32_t *off_tmp, uint32_t *total_dev, void *scan_temp,
+                     cudaStream_t s);
+void launch_ref_index_to_int64(const uint32_t *keys, const uint32_t *vals, long long M,
+                               long long *out, cudaStream_t s);
+
+// ---------------------------------------------------------------- D stage
+template <typename R>
+void launch_cphi(const Geom<R> &g, double *cphi, cudaStream_t s);
+template <typename R>
+void launch_d_pad(const typename Cx<R>::T *fhat, const double *cphi, typename Cx<R>::T *grid,
+                  const Geom<R> &g, cudaStream_t s);
+template <typename R>
+void launch_d_crop(const typename Cx<R>::T *grid, const double *cphi, typename Cx<R>::T *fhat,
+                   const Geom<R> &g, cudaStream_t s);
+
+// ---------------------------------------------------------------- B stage
+// tiled shared-memory kernels; return false when (d, w) has no tiled variant
+template <typename R>
+bool tiled_supported(int d, int w);
+template <typename R>
+size_t tiled_smem_bytes(const Geom<R> &g);
+template <typename R>
+void launch_b_tiled(const WorkItem *items, int nitems, const typename Cx<R>::T *grid,
+                    const R *xs, const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g,
+                    cudaStream_t s);
+template <typename R>
+void launch_bt_tiled(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
+                     const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g,
+                     cudaStream_t s);
+// generic global-memory kernels for any d and m
+template <typename R>
+void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,
+                      typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
+template <typename R>
+void launch_bt_generic(typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,
+                       const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
+
+// ---------------------------------------------------------------- NDFT
+template <typename R>
+void launch_ndft_trafo(const R *x, const typename Cx<R>::T *fhat, typename Cx<R>::T *f,
+                       const Geom<R> &g, cudaStream_t s);
+template <typename R>
+void launch_ndft_adjoint(const R *x, const typename Cx<R>::T *f, typename Cx<R>::T *fhat,
+                         const Geom<R> &g, cudaStream_t s);
+
+}  // namespace gb

@@ -284,7 +284,7 @@ def fft(data, sign, single=False):
 
 
 def bessel_i0(x, single=False):
-    return load(single).__getattr__(("orcf_" if single else "orc_") + "bessel_i0")(float(x))
+    return getattr(load(single), ("orcf_" if single else "orc_") + "bessel_i0")(float(x))
 
 
 # --- reading the reference's golden files (tests/data/nfft_*.txt format,

@@ -1,0 +1,273 @@
+"""GPU parity of the transform path through the C ABI (nfft_* / nfftf_*).
+
+Mirrors the reference's own test strategy (tests/nfft.c): golden files with
+the reference's init variants and error bound, online cases against the NDFT,
+plus bit-exact sorted index_x and element-wise agreement with the reference
+library's outputs (tests/golden/refrun.npz) and with the oracle.
+
+Tolerances: double plans agree with the reference to 1e-12 relative l2;
+single plans stay within 2x of the reference nfftf error against the FP64
+NDFT (plus 1e-7 absolute slack for rounding at tiny errors).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import (compare_adjoint, compare_trafo, default_guru_flags, err_direct_bound,
+                     err_trafo_bound, next_pow2, rel_l2, seeded_case)
+from nfft_gb300 import abi
+from nfft_gb300.plan import Plan
+
+pytestmark = pytest.mark.gpu
+
+
+def make_plan(lib, single, N, M, m=None, flags=None, init="guru", n=None):
+    if init == "guru":
+        if n is None:
+            n = [2 * next_pow2(v) for v in N]
+        if m is None:
+            m = 4 if single else 8
+        return Plan(lib, single, N, M, n=n, m=m,
+                    flags=default_guru_flags() if flags is None else flags)
+    return Plan(lib, single, N, M, init=init)
+
+
+def run_both(p, x, fh, f):
+    p.x[:] = x
+    p.precompute_one_psi()
+    p.f_hat[:] = fh
+    p.trafo()
+    out_f = p.f.copy()
+    p.f[:] = f
+    p.adjoint()
+    return out_f, p.f_hat.copy()
+
+
+def ndft(N, x, fh, f, m=8):
+    o = oracle.OraclePlan(N, len(x), m=m, single=False)
+    o.set_nodes(x)
+    return o.trafo_direct(fh), o.adjoint_direct(f)
+
+
+# ---------------------------------------------------------------- golden files
+INITS = ["dim", "default", "guru_pre_psi", "guru_pre_full_psi"]
+
+
+@pytest.mark.parametrize("single", [False, True])
+@pytest.mark.parametrize("init", INITS)
+def test_golden_files(gpulib, testdata, single, init):
+    """tests/nfft.c:691-708 init variants x trafo/adjoint on all 66 golden files."""
+    names = sorted({k.split("/")[0] for k in testdata})
+    for name in names:
+        N = [int(v) for v in testdata[name + "/N"]]
+        x = testdata[name + "/x"]
+        fh = testdata[name + "/f_hat"]
+        f = testdata[name + "/f"]
+        M = len(f)
+        d = len(N)
+        if init == "dim":
+            p = make_plan(gpulib, single, N, M, init="%dd" % d)
+        elif init == "default":
+            p = make_plan(gpulib, single, N, M, init="default")
+        else:
+            flags = default_guru_flags()
+            if init == "guru_pre_full_psi":
+                flags = (flags & ~abi.PRE_PSI) | abi.PRE_FULL_PSI
+            p = make_plan(gpulib, single, N, M, flags=flags)
+        p.x[:] = x
+        assert p.check() is None
+        p.precompute_one_psi()
+        if "adjoint" in name:
+            p.f[:] = f
+            p.adjoint()
+            err = compare_adjoint(p.f_hat.copy(), fh, f)
+        else:
+            p.f_hat[:] = fh
+            p.trafo()
+            err = compare_trafo(p.f.copy(), f, fh)
+        bound = err_trafo_bound(p.m, single)
+        p.finalize()
+        assert err < bound, (name, init, err, bound)
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_golden_files_direct(gpulib, testdata, single):
+    """trafo_direct / adjoint_direct on the golden files, bound 48 eps."""
+    names = sorted({k.split("/")[0] for k in testdata})
+    for name in names:
+        N = [int(v) for v in testdata[name + "/N"]]
+        x, fh, f = testdata[name + "/x"], testdata[name + "/f_hat"], testdata[name + "/f"]
+        M = len(f)
+        p = make_plan(gpulib, single, N, M, flags=default_guru_flags() & ~abi.PRE_PSI)
+        p.x[:] = x
+        if "adjoint" in name:
+            p.f[:] = f
+            p.adjoint_direct()
+            err = compare_adjoint(p.f_hat.copy(), fh, f)
+        else:
+            p.f_hat[:] = fh
+            p.trafo_direct()
+            err = compare_trafo(p.f.copy(), f, fh)
+        p.finalize()
+        assert err < err_direct_bound(single), (name, err)
+
+
+# ---------------------------------------------------------------- reference run
+def test_reference_run_parity(gpulib, refrun):
+    names = sorted({k.split("/")[0] for k in refrun if k.endswith("/trafo")})
+    for name in names:
+        meta = refrun[name + "/meta"]
+        m, single, N = int(meta[0]), bool(meta[1]), [int(v) for v in meta[2:]]
+        M = len(refrun[name + "/trafo"])
+        x, fh, f = seeded_case(N, M)
+        flags = default_guru_flags() | abi.NFFT_SORT_NODES
+        p = make_plan(gpulib, single, N, M, m=m, flags=flags)
+        gf, gfh = run_both(p, x, fh, f)
+        idx = p.index_x
+        cphi = np.concatenate(p.c_phi_inv)
+        p.finalize()
+        assert np.array_equal(idx, refrun[name + "/index_x"]), name
+        rf, rfh = refrun[name + "/trafo"], refrun[name + "/adjoint"]
+        if not single:
+            assert rel_l2(gf, rf) < 1e-12, (name, rel_l2(gf, rf))
+            assert rel_l2(gfh, rfh) < 1e-12, (name, rel_l2(gfh, rfh))
+            assert rel_l2(cphi, refrun[name + "/c_phi_inv"]) < 1e-14
+        else:
+            tf, tfh = ndft(N, x.astype(np.float32).astype(np.float64), fh.astype(np.complex64),
+                           f.astype(np.complex64))
+            e_ref, e_gpu = rel_l2(rf, tf), rel_l2(gf, tf)
+            assert e_gpu <= 2 * e_ref + 1e-7, (name, "trafo", e_gpu, e_ref)
+            e_ref, e_gpu = rel_l2(rfh, tfh), rel_l2(gfh, tfh)
+            assert e_gpu <= 2 * e_ref + 1e-7, (name, "adjoint", e_gpu, e_ref)
+
+
+# ---------------------------------------------------------------- online vs oracle
+CASES = [
+    # N, M, m, single
+    ([256], 3000, 8, False),
+    ([100], 700, 5, False),
+    ([64, 64], 5000, 6, False),
+    ([40, 24], 900, 7, False),
+    ([32, 32, 32], 6000, 4, False),
+    ([16, 16, 16], 500, 9, False),  # no tiled kernel for m=9: generic path
+    ([512], 20000, 4, True),
+    ([128, 128], 40000, 6, True),
+    ([64, 32], 3000, 3, True),
+    ([64, 64, 64], 100000, 4, True),
+    ([32, 48, 16], 20000, 6, True),
+    ([8, 8, 8, 8], 500, 3, False),  # d = 4: generic kernels and split FFT
+    ([6, 8, 4, 6, 4], 200, 2, True),  # d = 5
+]
+
+
+@pytest.mark.parametrize("N,M,m,single", CASES)
+def test_online_vs_oracle(gpulib, N, M, m, single):
+    x, fh, f = seeded_case(N, M, seed=11)
+    flags = default_guru_flags() | abi.NFFT_SORT_NODES
+    p = make_plan(gpulib, single, N, M, m=m, flags=flags)
+    gf, gfh = run_both(p, x, fh, f)
+    idx = p.index_x
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=[2 * next_pow2(v) for v in N], m=m, single=single)
+    o.set_nodes(x.astype(np.float32) if single else x)
+    o.precompute()
+    assert np.array_equal(idx, o.index_x())
+    od = oracle.OraclePlan(N, M, n=[2 * next_pow2(v) for v in N], m=m, single=False)
+    od.set_nodes(x.astype(np.float32).astype(np.float64) if single else x)
+    od.precompute()
+    rf = od.trafo(fh.astype(np.complex64) if single else fh)
+    rfh = od.adjoint(f.astype(np.complex64) if single else f)
+    tol = 2e-5 if single else 1e-12
+    assert rel_l2(gf, rf) < tol, rel_l2(gf, rf)
+    assert rel_l2(gfh, rfh) < tol, rel_l2(gfh, rfh)
+
+
+def test_clustered_nodes_and_heavy_tiles(gpulib):
+    """Nodes packed into a few tiles: many work items per tile, same results."""
+    rng = np.random.default_rng(5)
+    N, M, m = [32, 32, 32], 60000, 4
+    centres = rng.uniform(-0.5, 0.5, (4, 3))
+    x = centres[rng.integers(0, 4, M)] + 0.01 * rng.standard_normal((M, 3))
+    x = ((x + 0.5) % 1.0) - 0.5
+    fh = rng.uniform(-1, 1, 32 ** 3) + 1j * rng.uniform(-1, 1, 32 ** 3)
+    f = rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)
+    p = make_plan(gpulib, True, N, M, m=m)
+    gf, gfh = run_both(p, x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64))
+    p.finalize()
+    od = oracle.OraclePlan(N, M, n=[64] * 3, m=m, single=False)
+    od.set_nodes(x.astype(np.float32).astype(np.float64))
+    od.precompute()
+    assert rel_l2(gf, od.trafo(fh.astype(np.complex64))) < 2e-5
+    assert rel_l2(gfh, od.adjoint(f.astype(np.complex64))) < 2e-5
+
+
+def test_edge_nodes_and_small_m(gpulib):
+    """Nodes on -1/2 and just below +1/2, window wrap-around on every side."""
+    N, m = [32, 32], 6
+    edge = np.array([-0.5, -0.5 + 1e-12, 0.5 - 1e-12, 0.0, -1e-17, 0.25])
+    x = np.array(np.meshgrid(edge, edge)).reshape(2, -1).T.copy()
+    M = len(x)
+    rng = np.random.default_rng(2)
+    fh = rng.uniform(-1, 1, 1024) + 1j * rng.uniform(-1, 1, 1024)
+    f = rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)
+    for single in (False, True):
+        xx = x.astype(np.float32) if single else x
+        p = make_plan(gpulib, single, N, M, m=m, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+        gf, gfh = run_both(p, xx, fh, f)
+        idx = p.index_x
+        p.finalize()
+        o = oracle.OraclePlan(N, M, n=[64, 64], m=m, single=single)
+        o.set_nodes(xx)
+        o.precompute()
+        assert np.array_equal(idx, o.index_x())
+        tf, tfh = ndft(N, xx.astype(np.float64), fh, f)
+        bound = err_trafo_bound(m, single) * 10
+        assert compare_trafo(gf, tf, fh) < bound
+        assert compare_adjoint(gfh, tfh, f) < bound
+
+
+def test_single_node_and_direct_fallback(gpulib):
+    # M = 1, and N <= m forces the NDFT path (nfft.c:5658-5665)
+    for N, M, m in (([16, 16], 1, 6), ([4, 6], 30, 8), ([2], 5, 4)):
+        x, fh, f = seeded_case(N, M, seed=9)
+        p = make_plan(gpulib, False, N, M, m=m)
+        gf, gfh = run_both(p, x, fh, f)
+        p.finalize()
+        tf, tfh = ndft(N, x, fh, f)
+        assert rel_l2(gf, tf) < 1e-9
+        assert rel_l2(gfh, tfh) < 1e-9
+
+
+def test_check_messages(gpulib):
+    p = make_plan(gpulib, False, [16, 16], 10, m=4)
+    p.x[:] = 0.1
+    assert p.check() is None
+    p.x[3, 1] = 0.5
+    assert p.check() == "ths->x out of range [-0.5,0.5)"
+    p.finalize()
+    q = make_plan(gpulib, False, [15, 16], 10, m=4)
+    q.x[:] = 0.0
+    assert q.check() == "polynomial degree N has to be even"
+    q.finalize()
+
+
+def test_repeated_calls_and_no_precompute_flags(gpulib):
+    """Without PRE_*PSI flags the node set-up follows x on every call."""
+    N, M = [48, 48], 3000
+    x, fh, f = seeded_case(N, M, seed=21)
+    flags = abi.PRE_PHI_HUT | abi.MALLOC_X | abi.MALLOC_F | abi.MALLOC_F_HAT | abi.FFTW_INIT
+    p = make_plan(gpulib, False, N, M, m=6, flags=flags)
+    p.x[:] = x
+    p.f_hat[:] = fh
+    p.trafo()
+    a = p.f.copy()
+    p.trafo()
+    assert np.array_equal(a, p.f)
+    x2 = np.roll(x, 7, axis=0)
+    p.x[:] = x2
+    p.trafo()
+    b = p.f.copy()
+    p.finalize()
+    tf, _ = ndft(N, x2, fh, f)
+    assert rel_l2(b, tf) < 1e-9
+    assert rel_l2(b, np.roll(a, 7)) < 1e-12

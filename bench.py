@@ -1,0 +1,402 @@
+#!/usr/bin/env python3
+"""Benchmark of the NFFT transform path: nodes/s for one trafo + one adjoint.
+
+Workload (default): 3-D single-precision NFFT, N = 128^3, sigma = 2
+(n = 256^3), Kaiser-Bessel window m = 4, M = 2^24 nodes iid uniform in
+[-1/2, 1/2)^3 (seed 0), f_hat and the adjoint input with real and imaginary
+parts iid U(-1, 1).  A step is one nfftf_trafo plus one nfftf_adjoint over
+all M nodes; value = nodes per step / step time (whole job over all ranks).
+
+* value:  device-resident operands (gb_trafo_ptr / gb_adjoint_ptr), timed
+          with CUDA events on the plan's stream;
+* e2e:    the reference-facing C ABI (nfftf_trafo / nfftf_adjoint) on host
+          arrays, host<->device copies inside the timed region;
+* cpu_baseline / --impl reference: the oracle's OpenMP restatement of the
+          reference algorithm (PRE_PSI tables, sorted nodes, blockwise
+          adjoint) on this host's cores, on a bounded node sample.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "nodes/s fwd+adj, %HBM roofline; iNFFT time to 1e-5 rel. err: learned vs plain"
+UNIT = "nodes/s"
+CPU_SAMPLE_M = 1 << 20
+
+
+def workload(name):
+    if name == "small":  # for profiler captures of the same kernels
+        return dict(name="3-D NFFT FP32 N=64^3 n=128^3 m=4 M=2^21 uniform", d=3, N=[64] * 3,
+                    n=[128] * 3, m=4, M=1 << 21, dist="uniform")
+    dist = "clustered" if name == "clustered" else "uniform"
+    return dict(name="3-D NFFT FP32 N=128^3 n=256^3 m=4 M=2^24 %s" % dist, d=3, N=[128] * 3,
+                n=[256] * 3, m=4, M=1 << 24, dist=dist)
+
+
+def make_nodes(wl, seed):
+    rng = np.random.default_rng(seed)
+    M, d = wl["M"], wl["d"]
+    if wl["dist"] == "uniform":
+        x = rng.uniform(-0.5, 0.5, size=(M, d)).astype(np.float32)
+    else:  # mixture of 32 isotropic Gaussians, std 0.02, wrapped to the torus
+        c = rng.uniform(-0.5, 0.5, size=(32, d))
+        x = c[rng.integers(0, 32, M)] + 0.02 * rng.standard_normal((M, d))
+        x = (((x + 0.5) % 1.0) - 0.5).astype(np.float32)
+        x[x >= 0.5] = -0.5
+    return x
+
+
+def algorithmic_bytes_B(wl):
+    """Bytes of one B or B^T launch: nodes (d reals), samples (one complex)
+    and the oversampled grid once (FP32: r = 4, c = 8)."""
+    n_total = int(np.prod(wl["n"]))
+    return wl["M"] * (wl["d"] * 4 + 8) + n_total * 8
+
+
+def flops_B(wl):
+    w = 2 * wl["m"] + 2
+    return 4.0 * w ** wl["d"] * wl["M"]
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [v.strip() for v in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_pair(wl, x, sample_m, steps, warmup):
+    """Time the oracle's restatement of the reference (OpenMP, PRE_PSI,
+    sorted nodes, blockwise adjoint) on `sample_m` nodes of the workload with
+    the full grid; extrapolate B / B^T linearly in M, keep D and FFT as
+    measured (they do not depend on M).  Returns per-step dicts."""
+    import oracle
+    o = oracle.OraclePlan(wl["N"], sample_m, n=wl["n"], m=wl["m"], single=True, sort=True,
+                          blockwise=True, pre_psi=True)
+    o.set_nodes(x[:sample_m])
+    t0 = time.perf_counter()
+    o.precompute()
+    t_pre = time.perf_counter() - t0
+    rng = np.random.default_rng(1)
+    NN = int(np.prod(wl["N"]))
+    fh = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, sample_m) + 1j * rng.uniform(-1, 1, sample_m)).astype(np.complex64)
+    out = []
+    scale = wl["M"] / sample_m
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        o.trafo(fh)
+        t1 = time.perf_counter()
+        st_t = o.stage_times()
+        o.adjoint(f)
+        t2 = time.perf_counter()
+        st_a = o.stage_times()
+        fixed = st_t[0] + st_t[1] + st_a[0] + st_a[1]
+        b = st_t[2] + st_a[2]
+        full = fixed + b * scale
+        if it >= warmup:
+            out.append(dict(pair_s=t2 - t0, fixed_s=fixed, b_s=b, full_s=full,
+                            nodes_per_s=wl["M"] / full))
+    o.close()
+    return out, t_pre
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    x = make_nodes(wl, 0)
+    steps, t_pre = cpu_pair(wl, x, min(CPU_SAMPLE_M, wl["M"]), args.steps, args.warmup)
+    vals = [s["nodes_per_s"] for s in steps]
+    value = statistics.median(vals)
+    ms = statistics.mean(s["full_s"] for s in steps) * 1e3
+    cores = cpu_cores()
+    sample = ("oracle OpenMP restatement of the reference (PRE_PSI, sorted nodes, blockwise adjoint, "
+              "project radix-2 FFT) on the first %d of %d nodes with the full 256^3 grid; B and B^T "
+              "time scaled by M/%d, D and FFT as measured; %d threads"
+              % (CPU_SAMPLE_M, wl["M"], CPU_SAMPLE_M, cores))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(wl),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "precompute_s_sample": t_pre}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_of(wl):
+    return {"workload": wl["name"], "d": wl["d"], "N": wl["N"], "n": wl["n"], "m": wl["m"],
+            "M": wl["M"], "nodes": wl["dist"], "precision": "complex64",
+            "window": "Kaiser-Bessel", "l2_between_steps": "inputs larger than L2 (x 201 MB, "
+            "grid 134 MB, f 134 MB per rank); no flush"}
+
+
+# ------------------------------------------------------------------ GPU side
+def run_gpu(args, wl):
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import abi
+    from nfft_gb300.plan import Plan
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    lib = nfft_gb300.lib()
+    M, N, n, m = wl["M"], wl["N"], wl["n"], wl["m"]
+    NN = int(np.prod(N))
+    flags = (abi.PRE_PHI_HUT | abi.PRE_PSI | abi.MALLOC_X | abi.MALLOC_F_HAT | abi.MALLOC_F
+             | abi.FFTW_INIT | abi.FFT_OUT_OF_PLACE | abi.NFFT_SORT_NODES)
+    p = Plan(lib, True, N, M, n=n, m=m, flags=flags)
+    x = make_nodes(wl, rank)
+    p.x[:] = x
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p.precompute_one_psi()
+    t_pre = time.perf_counter() - t0
+
+    rng = np.random.default_rng(100 + rank)
+    fh_host = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f_host = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
+    dev = torch.device("cuda", local)
+    fh_in = torch.from_numpy(fh_host.view(np.float32)).to(dev)
+    f_in = torch.from_numpy(f_host.view(np.float32)).to(dev)
+    f_out = torch.empty(2 * M, dtype=torch.float32, device=dev)
+    fh_out = torch.empty(2 * NN, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    pp = C.byref(p.p)
+    lib.nfftf_gb_set_stream(pp, C.c_void_p(stream.cuda_stream))
+    trafo = lib.nfftf_gb_trafo_ptr
+    adjoint = lib.nfftf_gb_adjoint_ptr
+    trafo.argtypes = adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    pa = C.addressof(p.p)
+
+    def step():
+        trafo(pa, fh_in.data_ptr(), f_out.data_ptr())
+        adjoint(pa, f_in.data_ptr(), fh_out.data_ptr())
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident)
+    begin = lib.nfftf_gb_timing_begin
+    begin.argtypes = [C.c_void_p, C.c_int]
+    end = lib.nfftf_gb_timing_end
+    end.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    begin(pa, 2 * args.steps)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    sums = (C.c_float * 7)()
+    counts = (C.c_int * 2)()
+    end(pa, sums, counts)
+    launches = 4 * args.steps  # d_pad + b_tiled (trafo), bt_tiled + d_crop (adjoint)
+    if dist is not None:
+        t = torch.tensor([ms_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = M * world / (ms_step * 1e-3)
+
+    # ---- e2e through the C ABI on host arrays (copies inside the timed region)
+    e2e_times = []
+    for it in range(args.warmup + args.steps):
+        p.f_hat[:] = fh_host
+        barrier()
+        t0 = time.perf_counter()
+        p.trafo()
+        p.adjoint()
+        t1 = time.perf_counter()
+        if it >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = M * world / e2e_s
+    h2d = NN * 8 + M * 8
+    d2h = M * 8 + NN * 8
+
+    # ---- roofline of the dominant kernel
+    nT, nA = max(counts[0], 1), max(counts[1], 1)
+    stage = {"trafo_D_ms": sums[0] / nT, "trafo_FFT_ms": sums[1] / nT, "trafo_B_ms": sums[2] / nT,
+             "adjoint_memset_ms": sums[3] / nA, "adjoint_BT_ms": sums[4] / nA,
+             "adjoint_FFT_ms": sums[5] / nA, "adjoint_DT_ms": sums[6] / nA}
+    b_ms, bt_ms = stage["trafo_B_ms"], stage["adjoint_BT_ms"]
+    dom, dom_ms = ("bt_tiled (B^T spreading)", bt_ms) if bt_ms >= b_ms else ("b_tiled (B interpolation)", b_ms)
+    peaks, peak_kind = measured_peaks()
+    bytes_b = algorithmic_bytes_B(wl)
+    achieved = bytes_b / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            tr = json.load(fh)
+        key = ("bt_tiled" if bt_ms >= b_ms else "b_tiled") + "/" + wl["dist"]
+        traffic = tr.get(key)
+    except Exception:
+        pass
+    fp32_peak = 152 * 128 * 2 * (clk["sm_mhz"] if clk else 1900.0) * 1e6 / 1e12
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 5), "traffic": traffic,
+            "kernel": dom, "algorithmic_bytes_per_launch": bytes_b, "launch_ms": round(dom_ms, 4),
+            "peak_source": peak_kind,
+            "fp32_issue": {"flops_per_launch": flops_B(wl),
+                           "achieved_tflops": round(flops_B(wl) / (dom_ms * 1e-3) / 1e12, 3),
+                           "peak_tflops_at_clock": round(fp32_peak, 1),
+                           "frac": round(flops_B(wl) / (dom_ms * 1e-3) / 1e12 / fp32_peak, 4)}}
+    pair_bytes = 2 * (bytes_b + 2 * int(np.prod(n)) * 8 + (NN + int(np.prod(n))) * 8)
+    hbm_pair = pair_bytes / (ms_step * 1e-3) / 1e9
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        steps, _ = cpu_pair(wl, x, min(CPU_SAMPLE_M, M), 2, 1)
+        v = statistics.median(s["nodes_per_s"] for s in steps)
+        cpu = {"value": v, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+               "sample": "oracle OpenMP restatement of the reference on the first %d nodes with the "
+                         "full grid; B/B^T scaled by M/%d, D and FFT as measured" % (CPU_SAMPLE_M, CPU_SAMPLE_M)}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(config_of(wl), parallelism="replicas x%d" % world),
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+            "clocks": clk, "gpu_launches": launches,
+            "stages_ms": {k: round(v, 4) for k, v in stage.items()},
+            "pair_hbm_gbs_algorithmic": round(hbm_pair, 1),
+            "pair_hbm_frac": round(hbm_pair / peaks["hbm_gbs"], 4),
+            "precompute_s": round(t_pre, 4)}
+    p.finalize()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "clustered", "small"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    wl = workload(args.workload)
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -34,14 +34,48 @@ void X(gb_precompute_device)(X(plan) *ths); \
  * not synchronise and do not touch the host arrays. */ \
 void X(gb_trafo_device)(X(plan) *ths); \
 void X(gb_adjoint_device)(X(plan) *ths); \
+/* The same on caller-owned device vectors: f_hat_dev (N_total complex) and \
+ * f_dev (M_total complex) in the caller's natural orders. */ \
+void X(gb_trafo_ptr)(X(plan) *ths, const void *f_hat_dev, void *f_dev); \
+void X(gb_adjoint_ptr)(X(plan) *ths, const void *f_dev, void *f_hat_dev); \
 /* Milliseconds of the last host-API transform per stage: \
- * [0] D or D^T, [1] FFT, [2] B or B^T, [3] host<->device copies. */ \
+ * [0] D or D^T, [1] FFT, [2] B or B^T kernel, [3] the rest (copies, the \
+ * grid memset of B^T). */ \
 void X(gb_stage_times)(X(plan) *ths, float *ms4); \
+/* The same for the last device transform (waits for it to finish). */ \
+void X(gb_device_stage_times)(X(plan) *ths, float *ms4); \
 /* Kernel launches of the last transform (library kernels, not cuFFT). */ \
-int X(gb_last_launch_count)(X(plan) *ths);
+int X(gb_last_launch_count)(X(plan) *ths); \
+/* Time up to max_calls following device transforms with CUDA events on the \
+ * plan's stream, without synchronising between them.  timing_end waits for \
+ * them and returns the number of calls timed; sums7 (ms) = trafo D, trafo \
+ * FFT, trafo B, adjoint grid memset, adjoint B^T, adjoint FFT, adjoint D^T; \
+ * counts2 = trafo calls, adjoint calls. */ \
+int X(gb_timing_begin)(X(plan) *ths, int max_calls); \
+int X(gb_timing_end)(X(plan) *ths, float *sums7, int *counts2);
 
 NFFTGB_DEFINE_API(NFFT_MANGLE_DOUBLE)
 NFFTGB_DEFINE_API(NFFT_MANGLE_FLOAT)
+
+/* Solver extensions (solver_gb_* for double, solverf_gb_* for float).  They
+ * apply when the solver's mv plan is an nfft plan of this library, whose
+ * iteration then runs in HBM; they return -1 for any other mv plan. */
+#define NFFTGB_DEFINE_SOLVER_API(X) \
+/* Which vectors each before_loop / loop_one_step call copies back to the \
+ * host struct: 2 = all (default, the reference's visible state), \
+ * 1 = f_hat_iter and r_iter, 0 = scalars only. */ \
+int X(gb_set_sync)(X(plan_complex) *ths, int level); \
+/* Copy every iterate vector back to the host struct now. */ \
+int X(gb_sync)(X(plan_complex) *ths); \
+/* Recompute r = y - A f_hat_iter with an FP64 transform every `every` \
+ * iterations (single-precision solvers; 0 = off). */ \
+int X(gb_set_refresh)(X(plan_complex) *ths, int every); \
+/* Device copies of f_hat_iter (N_total complex) and y (M_total complex). */ \
+void *X(gb_device_f_hat_iter)(X(plan_complex) *ths); \
+void *X(gb_device_y)(X(plan_complex) *ths);
+
+NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_DOUBLE)
+NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_FLOAT)
 
 /* Last error message recorded by the library (empty string if none).  Fatal
  * errors also go through nfft_die / nfft_die_hook like the reference. */

@@ -50,7 +50,8 @@ def build(force=False, verbose=False, ptxas_v=False, jobs=None):
     """Compile and link; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
-    hdr = max(_deps_mtime(), os.path.getmtime(os.path.join(ROOT, "include", "nfft3.h")))
+    inc = os.path.join(ROOT, "include")
+    hdr = max([_deps_mtime()] + [os.path.getmtime(os.path.join(inc, f)) for f in os.listdir(inc)])
     extra = ["-Xptxas", "-v"] if ptxas_v else []
     todo = [s for s in srcs if force or ptxas_v or not os.path.exists(_obj(s))
             or os.path.getmtime(_obj(s)) < max(os.path.getmtime(s), hdr)]

@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "../../include/nfft3.h"
 #include "gb_internal.h"
@@ -80,7 +81,14 @@ struct Ctx {
   int nitems = 0;
   int ntiles = 1;
   bool nodes_ready = false;
-  cudaEvent_t ev[5] = {};
+  cudaEvent_t ev[7] = {};
+  // optional per-call event ring for timing a sequence of device calls
+  std::vector<cudaEvent_t> ring;  // 7 events per slot
+  std::vector<char> ring_kind;    // 1 = trafo, 0 = adjoint
+  int ring_slots = 0, ring_used = 0;
+  bool ring_on = false;
+  bool last_trafo = true;
+  bool timed = false;
   float stage_ms[4] = {0, 0, 0, 0};
   int launches = 0;
 };
@@ -279,7 +287,7 @@ static void init_help(typename Api<R>::plan *ths)
 
   GB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->own_stream = true;
-  for (int i = 0; i < 5; ++i) GB_CUDA(cudaEventCreate(&c->ev[i]));
+  for (int i = 0; i < 7; ++i) GB_CUDA(cudaEventCreate(&c->ev[i]));
   const size_t M = (size_t)std::max<long long>(g.M, 1);
   dev_alloc<R>((void **)&c->x_dev, M * d * sizeof(R));
   dev_alloc<R>((void **)&c->fhat_dev, (size_t)g.N_total * sizeof(C));
@@ -415,76 +423,159 @@ static void ensure_nodes(typename Api<R>::plan *ths, Ctx<R> *c)
 }
 
 // ------------------------------------------------------------ transforms
+// Events: ev[0] call start, ev[1] stage 1 start, ev[6] after the grid
+// memset of B^T, ev[2] stage 1 end, ev[3] FFT end, ev[4] stage 3 end,
+// ev[5] call end (after the result copy).
 template <typename R>
-static void b_stage(Ctx<R> *c)
+static void b_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
-  if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, c->f_dev, c->g, c->stream);
-  else launch_b_generic<R>(c->grid, c->xs, c->perm, c->f_dev, c->g, c->stream);
+  if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  else launch_b_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
 
 template <typename R>
-static void bt_stage(Ctx<R> *c)
+static cudaEvent_t *events_for_call(Ctx<R> *c, bool trafo)
+{
+  if (c->ring_on && c->ring_used < c->ring_slots) {
+    c->ring_kind[c->ring_used] = trafo ? 1 : 0;
+    return &c->ring[7 * (size_t)c->ring_used++];
+  }
+  return c->ev;
+}
+
+template <typename R>
+static void bt_stage(Ctx<R> *c, const typename Cx<R>::T *f, cudaEvent_t *E)
 {
   GB_CUDA(cudaMemsetAsync(c->grid, 0, (size_t)c->g.n_total * sizeof(typename Cx<R>::T), c->stream));
-  if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, c->f_dev, c->g, c->stream);
-  else launch_bt_generic<R>(c->grid, c->xs, c->perm, c->f_dev, c->g, c->stream);
+  GB_CUDA(cudaEventRecord(E[6], c->stream));
+  if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  else launch_bt_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
 
-// f_dev = A fhat_dev, all on the device
+// f = A fhat, device vectors
 template <typename R>
-static void trafo_device(Ctx<R> *c)
+static void trafo_device(Ctx<R> *c, const typename Cx<R>::T *fhat, typename Cx<R>::T *f)
 {
+  c->last_trafo = true;
+  c->timed = !c->direct;
   if (c->direct) {
-    launch_ndft_trafo<R>(c->x_dev, c->fhat_dev, c->f_dev, c->g, c->stream);
+    launch_ndft_trafo<R>(c->x_dev, fhat, f, c->g, c->stream);
     c->launches = 1;
     return;
   }
-  GB_CUDA(cudaEventRecord(c->ev[1], c->stream));
-  launch_d_pad<R>(c->fhat_dev, c->cphi, c->grid, c->g, c->stream);
-  GB_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  cudaEvent_t *E = events_for_call(c, true);
+  GB_CUDA(cudaEventRecord(E[1], c->stream));
+  launch_d_pad<R>(fhat, c->cphi, c->grid, c->g, c->stream);
+  GB_CUDA(cudaEventRecord(E[2], c->stream));
   run_fft<R>(c, CUFFT_FORWARD);
-  GB_CUDA(cudaEventRecord(c->ev[3], c->stream));
-  b_stage<R>(c);
-  GB_CUDA(cudaEventRecord(c->ev[4], c->stream));
+  GB_CUDA(cudaEventRecord(E[3], c->stream));
+  b_stage<R>(c, f);
+  GB_CUDA(cudaEventRecord(E[4], c->stream));
   c->launches = 2;
 }
 
-// fhat_dev = A^H f_dev
+// fhat = A^H f, device vectors
 template <typename R>
-static void adjoint_device(Ctx<R> *c)
+static void adjoint_device(Ctx<R> *c, const typename Cx<R>::T *f, typename Cx<R>::T *fhat)
 {
+  c->last_trafo = false;
+  c->timed = !c->direct;
   if (c->direct) {
-    launch_ndft_adjoint<R>(c->x_dev, c->f_dev, c->fhat_dev, c->g, c->stream);
+    launch_ndft_adjoint<R>(c->x_dev, f, fhat, c->g, c->stream);
     c->launches = 1;
     return;
   }
-  GB_CUDA(cudaEventRecord(c->ev[1], c->stream));
-  bt_stage<R>(c);
-  GB_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  cudaEvent_t *E = events_for_call(c, false);
+  GB_CUDA(cudaEventRecord(E[1], c->stream));
+  bt_stage<R>(c, f, E);
+  GB_CUDA(cudaEventRecord(E[2], c->stream));
   run_fft<R>(c, CUFFT_INVERSE);
-  GB_CUDA(cudaEventRecord(c->ev[3], c->stream));
-  launch_d_crop<R>(c->grid, c->cphi, c->fhat_dev, c->g, c->stream);
-  GB_CUDA(cudaEventRecord(c->ev[4], c->stream));
+  GB_CUDA(cudaEventRecord(E[3], c->stream));
+  launch_d_crop<R>(c->grid, c->cphi, fhat, c->g, c->stream);
+  GB_CUDA(cudaEventRecord(E[4], c->stream));
   c->launches = 2;
 }
 
+// Stage times of the last transform (the caller has synchronised or the
+// events are waited on here): [0] D or D^T, [1] FFT, [2] B or B^T (kernel
+// only, without the grid memset), [3] the rest of the call (copies, memset).
 template <typename R>
-static void finish_times(typename Api<R>::plan *ths, Ctx<R> *c, bool trafo)
+static void stage_times(Ctx<R> *c, bool host_call)
 {
-  if (c->direct) {
-    ths->MEASURE_TIME_t[0] = ths->MEASURE_TIME_t[1] = ths->MEASURE_TIME_t[2] = 0;
+  if (!c->timed) {
+    for (int i = 0; i < 4; ++i) c->stage_ms[i] = 0;
     return;
   }
-  float a = 0, b = 0, d = 0, tot = 0;
+  GB_CUDA(cudaEventSynchronize(c->ev[host_call ? 5 : 4]));
+  float a = 0, b = 0, d = 0, tot = 0, ms = 0;
   GB_CUDA(cudaEventElapsedTime(&a, c->ev[1], c->ev[2]));
   GB_CUDA(cudaEventElapsedTime(&b, c->ev[2], c->ev[3]));
   GB_CUDA(cudaEventElapsedTime(&d, c->ev[3], c->ev[4]));
-  GB_CUDA(cudaEventElapsedTime(&tot, c->ev[0], c->ev[4]));
-  // trafo: D, FFT, B; adjoint: B^T, FFT, D^T
-  c->stage_ms[0] = trafo ? a : d;
+  if (!c->last_trafo) GB_CUDA(cudaEventElapsedTime(&ms, c->ev[1], c->ev[6]));
+  if (host_call) GB_CUDA(cudaEventElapsedTime(&tot, c->ev[0], c->ev[5]));
+  else GB_CUDA(cudaEventElapsedTime(&tot, c->ev[1], c->ev[4]));
+  c->stage_ms[0] = c->last_trafo ? a : d;
   c->stage_ms[1] = b;
-  c->stage_ms[2] = trafo ? d : a;
-  c->stage_ms[3] = std::max(0.0f, tot - a - b - d);
+  c->stage_ms[2] = c->last_trafo ? d : a - ms;
+  c->stage_ms[3] = std::max(0.0f, tot - a - b - d + ms);
+}
+
+// Per-call event ring: time a sequence of device transforms on the plan's
+// stream without synchronising between them.
+template <typename R>
+static int timing_begin(Ctx<R> *c, int max_calls)
+{
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  if (max_calls > c->ring_slots) {
+    for (int i = 7 * c->ring_slots; i < 7 * max_calls; ++i) {
+      cudaEvent_t e;
+      GB_CUDA(cudaEventCreate(&e));
+      c->ring.push_back(e);
+    }
+    c->ring_slots = max_calls;
+    c->ring_kind.resize(max_calls);
+  }
+  c->ring_used = 0;
+  c->ring_on = true;
+  return 0;
+}
+
+// sums[7] (ms): trafo D, trafo FFT, trafo B, adjoint memset, adjoint B^T,
+// adjoint FFT, adjoint D^T; counts[2]: trafo calls, adjoint calls
+template <typename R>
+static int timing_end(Ctx<R> *c, float *sums, int *counts)
+{
+  c->ring_on = false;
+  for (int i = 0; i < 7; ++i) sums[i] = 0;
+  counts[0] = counts[1] = 0;
+  for (int k = 0; k < c->ring_used; ++k) {
+    cudaEvent_t *E = &c->ring[7 * (size_t)k];
+    GB_CUDA(cudaEventSynchronize(E[4]));
+    float a = 0, b = 0, d = 0, ms = 0;
+    GB_CUDA(cudaEventElapsedTime(&a, E[1], E[2]));
+    GB_CUDA(cudaEventElapsedTime(&b, E[2], E[3]));
+    GB_CUDA(cudaEventElapsedTime(&d, E[3], E[4]));
+    if (c->ring_kind[k]) {
+      sums[0] += a;
+      sums[1] += b;
+      sums[2] += d;
+      counts[0]++;
+    } else {
+      GB_CUDA(cudaEventElapsedTime(&ms, E[1], E[6]));
+      sums[3] += ms;
+      sums[4] += a - ms;
+      sums[5] += b;
+      sums[6] += d;
+      counts[1]++;
+    }
+  }
+  return c->ring_used;
+}
+
+template <typename R>
+static void finish_times(typename Api<R>::plan *ths, Ctx<R> *c)
+{
+  stage_times<R>(c, true);
   // MEASURE_TIME_t[0] = D, [1] = FFT, [2] = B, in seconds (include/infft.h:1376-1410)
   ths->MEASURE_TIME_t[0] = (R)(c->stage_ms[0] * 1e-3);
   ths->MEASURE_TIME_t[1] = (R)(c->stage_ms[1] * 1e-3);
@@ -502,13 +593,13 @@ static void trafo(typename Api<R>::plan *ths)
   if (c->g.N_total > 0)
     GB_CUDA(cudaMemcpyAsync(c->fhat_dev, ths->f_hat, (size_t)c->g.N_total * sizeof(C),
                             cudaMemcpyHostToDevice, c->stream));
-  trafo_device<R>(c);
+  trafo_device<R>(c, c->fhat_dev, c->f_dev);
   if (c->g.M > 0)
     GB_CUDA(cudaMemcpyAsync(ths->f, c->f_dev, (size_t)c->g.M * sizeof(C), cudaMemcpyDeviceToHost,
                             c->stream));
-  GB_CUDA(cudaEventRecord(c->ev[4], c->stream));
+  GB_CUDA(cudaEventRecord(c->ev[5], c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
-  finish_times<R>(ths, c, true);
+  finish_times<R>(ths, c);
 }
 
 template <typename R>
@@ -522,13 +613,13 @@ static void adjoint(typename Api<R>::plan *ths)
   if (c->g.M > 0)
     GB_CUDA(cudaMemcpyAsync(c->f_dev, ths->f, (size_t)c->g.M * sizeof(C), cudaMemcpyHostToDevice,
                             c->stream));
-  adjoint_device<R>(c);
+  adjoint_device<R>(c, c->f_dev, c->fhat_dev);
   if (c->g.N_total > 0)
     GB_CUDA(cudaMemcpyAsync(ths->f_hat, c->fhat_dev, (size_t)c->g.N_total * sizeof(C),
                             cudaMemcpyDeviceToHost, c->stream));
-  GB_CUDA(cudaEventRecord(c->ev[4], c->stream));
+  GB_CUDA(cudaEventRecord(c->ev[5], c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
-  finish_times<R>(ths, c, false);
+  finish_times<R>(ths, c);
 }
 
 template <typename R>
@@ -600,8 +691,9 @@ static void finalize(typename Api<R>::plan *ths)
     cudaFree(c->cphi);
     cudaFree(c->tile_start);
     cudaFree(c->items);
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 7; ++i)
       if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (cudaEvent_t e : c->ring) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     ths->my_fftw_plan1 = nullptr;
@@ -752,42 +844,46 @@ extern "C" {
   {                                                                                                \
     Ctx<R> *c = ctx_of<R>(ths);                                                                    \
     if (!c->nodes_ready) nodes_from_device<R>(ths, c);                                             \
-    GB_CUDA(cudaEventRecord(c->ev[0], c->stream));                                                 \
-    trafo_device<R>(c);                                                                            \
+    trafo_device<R>(c, c->fhat_dev, c->f_dev);                                                     \
   }                                                                                                \
   void X##gb_adjoint_device(X##plan *ths)                                                          \
   {                                                                                                \
     Ctx<R> *c = ctx_of<R>(ths);                                                                    \
     if (!c->nodes_ready) nodes_from_device<R>(ths, c);                                             \
-    GB_CUDA(cudaEventRecord(c->ev[0], c->stream));                                                 \
-    adjoint_device<R>(c);                                                                          \
+    adjoint_device<R>(c, c->f_dev, c->fhat_dev);                                                   \
+  }                                                                                                \
+  void X##gb_trafo_ptr(X##plan *ths, const void *f_hat_dev, void *f_dev)                           \
+  {                                                                                                \
+    Ctx<R> *c = ctx_of<R>(ths);                                                                    \
+    if (!c->nodes_ready) nodes_from_device<R>(ths, c);                                             \
+    trafo_device<R>(c, (const Cx<R>::T *)f_hat_dev, (Cx<R>::T *)f_dev);                            \
+  }                                                                                                \
+  void X##gb_adjoint_ptr(X##plan *ths, const void *f_dev, void *f_hat_dev)                         \
+  {                                                                                                \
+    Ctx<R> *c = ctx_of<R>(ths);                                                                    \
+    if (!c->nodes_ready) nodes_from_device<R>(ths, c);                                             \
+    adjoint_device<R>(c, (const Cx<R>::T *)f_dev, (Cx<R>::T *)f_hat_dev);                          \
   }                                                                                                \
   void X##gb_stage_times(X##plan *ths, float *ms4)                                                 \
   {                                                                                                \
     Ctx<R> *c = ctx_of<R>(ths);                                                                    \
     for (int i = 0; i < 4; ++i) ms4[i] = c->stage_ms[i];                                           \
   }                                                                                                \
-  int X##gb_last_launch_count(X##plan *ths) { return ctx_of<R>(ths)->launches; }
+  void X##gb_device_stage_times(X##plan *ths, float *ms4)                                          \
+  {                                                                                                \
+    Ctx<R> *c = ctx_of<R>(ths);                                                                    \
+    stage_times<R>(c, false);                                                                      \
+    for (int i = 0; i < 4; ++i) ms4[i] = c->stage_ms[i];                                           \
+  }                                                                                                \
+  int X##gb_last_launch_count(X##plan *ths) { return ctx_of<R>(ths)->launches; }                  \
+  int X##gb_timing_begin(X##plan *ths, int max_calls) { return timing_begin<R>(ctx_of<R>(ths), max_calls); } \
+  int X##gb_timing_end(X##plan *ths, float *sums7, int *counts2)                                    \
+  {                                                                                                \
+    return timing_end<R>(ctx_of<R>(ths), sums7, counts2);                                          \
+  }
 
 GB_PLAN_API(nfft_, double, 8)
 GB_PLAN_API(nfftf_, float, 4)
 
 }  // extern "C"
 
-// entry points used by the solver translation unit
-namespace gb {
-template <typename R>
-void plan_trafo_device(typename Api<R>::plan *ths)
-{
-  Ctx<R> *c = ctx_of<R>(ths);
-  if (!c->nodes_ready) nodes_from_device<R>(ths, c);
-  trafo_device<R>(c);
-}
-template <typename R>
-void plan_adjoint_device(typename Api<R>::plan *ths)
-{
-  Ctx<R> *c = ctx_of<R>(ths);
-  if (!c->nodes_ready) nodes_from_device<R>(ths, c);
-  adjoint_device<R>(c);
-}
-}  // namespace gb

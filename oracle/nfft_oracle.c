@@ -410,6 +410,18 @@ static void D_T(orc_plan *p, R *fhat)
 /* B_openmp_A nfft.c:1172-1278).  Nodes run in sorted order when the sort is */
 /* on (nfft_trafo_2d_B nfft.c:3221-3410).                                    */
 /* ------------------------------------------------------------------------- */
+/* per node: window values ps[t] and wrapped grid indices idx[t][l] */
+static void node_taps(const orc_plan *p, INT j, const R **ps, INT (*idx)[64], R *scratch)
+{
+  const int w = 2 * p->m + 2;
+  int t, l;
+  for (t = 0; t < p->d; t++) {
+    const INT u = node_u(p, j, t), n = p->n[t];
+    ps[t] = psi_of(p, j, t, scratch + 64 * t);
+    for (l = 0; l < w; l++) idx[t][l] = (((u + l) % n) + n) % n;
+  }
+}
+
 static void B_A(orc_plan *p, R *f)
 {
   const int d = p->d, w = 2 * p->m + 2;
@@ -419,34 +431,64 @@ static void B_A(orc_plan *p, R *f)
 #endif
   {
     R scratch[8 * 64];
+    INT idx[8][64];
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
     for (jj = 0; jj < p->M; jj++) {
       const INT j = p->index_x ? p->index_x[2 * jj + 1] : jj;
       const R *ps[8];
-      INT u[8], l[8];
       R sr = 0, si = 0;
-      int t;
-      for (t = 0; t < d; t++) {
-        ps[t] = psi_of(p, j, t, scratch + 64 * t);
-        u[t] = node_u(p, j, t);
-        l[t] = 0;
-      }
+      int l0, l1, l2;
+      node_taps(p, j, ps, idx, scratch);
       if (d == 1) {
-        for (l[0] = 0; l[0] < w; l[0]++) {
-          INT i0 = ((u[0] + l[0]) % p->n[0] + p->n[0]) % p->n[0];
-          sr += ps[0][l[0]] * p->g[2 * i0];
-          si += ps[0][l[0]] * p->g[2 * i0 + 1];
+        for (l0 = 0; l0 < w; l0++) {
+          const R *gv = p->g + 2 * idx[0][l0];
+          sr += ps[0][l0] * gv[0];
+          si += ps[0][l0] * gv[1];
+        }
+      } else if (d == 2) {
+        const INT n1 = p->n[1];
+        for (l0 = 0; l0 < w; l0++) {
+          const R *g0 = p->g + 2 * idx[0][l0] * n1;
+          R tr = 0, ti = 0;
+          for (l1 = 0; l1 < w; l1++) {
+            const R *gv = g0 + 2 * idx[1][l1];
+            tr += ps[1][l1] * gv[0];
+            ti += ps[1][l1] * gv[1];
+          }
+          sr += ps[0][l0] * tr;
+          si += ps[0][l0] * ti;
+        }
+      } else if (d == 3) {
+        const INT n1 = p->n[1], n2 = p->n[2];
+        for (l0 = 0; l0 < w; l0++) {
+          const R *g0 = p->g + 2 * idx[0][l0] * n1 * n2;
+          R ur = 0, ui = 0;
+          for (l1 = 0; l1 < w; l1++) {
+            const R *g01 = g0 + 2 * idx[1][l1] * n2;
+            R tr = 0, ti = 0;
+            for (l2 = 0; l2 < w; l2++) {
+              const R *gv = g01 + 2 * idx[2][l2];
+              tr += ps[2][l2] * gv[0];
+              ti += ps[2][l2] * gv[1];
+            }
+            ur += ps[1][l1] * tr;
+            ui += ps[1][l1] * ti;
+          }
+          sr += ps[0][l0] * ur;
+          si += ps[0][l0] * ui;
         }
       } else {
         /* odometer over the w^d tensor product, last dim fastest */
+        INT l[8];
+        int t;
+        for (t = 0; t < d; t++) l[t] = 0;
         for (;;) {
           INT pos = 0;
           R wgt = (R)1.0;
           for (t = 0; t < d; t++) {
-            INT it = ((u[t] + l[t]) % p->n[t] + p->n[t]) % p->n[t];
-            pos = pos * p->n[t] + it;
+            pos = pos * p->n[t] + idx[t][l[t]];
             wgt *= ps[t][l[t]];
           }
           sr += wgt * p->g[2 * pos];
@@ -476,30 +518,71 @@ static void spread_node(orc_plan *p, INT j, const R *f, INT row_lo, INT row_hi,
 {
   const int d = p->d, w = 2 * p->m + 2;
   const R *ps[8];
-  INT u[8], l[8];
-  int t;
-  for (t = 0; t < d; t++) {
-    ps[t] = psi_of(p, j, t, scratch + 64 * t);
-    u[t] = node_u(p, j, t);
-    l[t] = 0;
-  }
-  for (;;) {
-    INT pos = 0, i0 = ((u[0] + l[0]) % p->n[0] + p->n[0]) % p->n[0];
-    if (i0 >= row_lo && i0 < row_hi) {
-      R wgt = (R)1.0;
-      for (t = 0; t < d; t++) {
-        INT it = ((u[t] + l[t]) % p->n[t] + p->n[t]) % p->n[t];
-        pos = pos * p->n[t] + it;
-        wgt *= ps[t][l[t]];
+  INT idx[8][64];
+  const R fr = f[2 * j], fi = f[2 * j + 1];
+  int l0, l1, l2;
+  node_taps(p, j, ps, idx, scratch);
+  if (d == 1) {
+    for (l0 = 0; l0 < w; l0++) {
+      R *gv;
+      if (idx[0][l0] < row_lo || idx[0][l0] >= row_hi) continue;
+      gv = p->g + 2 * idx[0][l0];
+      gv[0] += ps[0][l0] * fr;
+      gv[1] += ps[0][l0] * fi;
+    }
+  } else if (d == 2) {
+    const INT n1 = p->n[1];
+    for (l0 = 0; l0 < w; l0++) {
+      R *g0;
+      R wr, wi;
+      if (idx[0][l0] < row_lo || idx[0][l0] >= row_hi) continue;
+      g0 = p->g + 2 * idx[0][l0] * n1;
+      wr = ps[0][l0] * fr;
+      wi = ps[0][l0] * fi;
+      for (l1 = 0; l1 < w; l1++) {
+        R *gv = g0 + 2 * idx[1][l1];
+        gv[0] += ps[1][l1] * wr;
+        gv[1] += ps[1][l1] * wi;
       }
-      p->g[2 * pos] += wgt * f[2 * j];
-      p->g[2 * pos + 1] += wgt * f[2 * j + 1];
     }
-    for (t = d - 1; t >= 0; t--) {
-      if (++l[t] < w) break;
-      l[t] = 0;
+  } else if (d == 3) {
+    const INT n1 = p->n[1], n2 = p->n[2];
+    for (l0 = 0; l0 < w; l0++) {
+      R *g0;
+      if (idx[0][l0] < row_lo || idx[0][l0] >= row_hi) continue;
+      g0 = p->g + 2 * idx[0][l0] * n1 * n2;
+      for (l1 = 0; l1 < w; l1++) {
+        R *g01 = g0 + 2 * idx[1][l1] * n2;
+        const R w01 = ps[0][l0] * ps[1][l1];
+        const R wr = w01 * fr, wi = w01 * fi;
+        for (l2 = 0; l2 < w; l2++) {
+          R *gv = g01 + 2 * idx[2][l2];
+          gv[0] += ps[2][l2] * wr;
+          gv[1] += ps[2][l2] * wi;
+        }
+      }
     }
-    if (t < 0) break;
+  } else {
+    INT l[8];
+    int t;
+    for (t = 0; t < d; t++) l[t] = 0;
+    for (;;) {
+      if (idx[0][l[0]] >= row_lo && idx[0][l[0]] < row_hi) {
+        INT pos = 0;
+        R wgt = (R)1.0;
+        for (t = 0; t < d; t++) {
+          pos = pos * p->n[t] + idx[t][l[t]];
+          wgt *= ps[t][l[t]];
+        }
+        p->g[2 * pos] += wgt * fr;
+        p->g[2 * pos + 1] += wgt * fi;
+      }
+      for (t = d - 1; t >= 0; t--) {
+        if (++l[t] < w) break;
+        l[t] = 0;
+      }
+      if (t < 0) break;
+    }
   }
 }
 

@@ -75,7 +75,12 @@ def test_golden_files(gpulib, testdata, single, init):
                 flags = (flags & ~abi.PRE_PSI) | abi.PRE_FULL_PSI
             p = make_plan(gpulib, single, N, M, flags=flags)
         p.x[:] = x
-        assert p.check() is None
+        if p.check() is not None:
+            # the reference counts a case its nfft_check rejects (odd N) as
+            # passed without running it (tests/nfft.c:315-325)
+            assert N[0] % 2 == 1, (name, p.check())
+            p.finalize()
+            continue
         p.precompute_one_psi()
         if "adjoint" in name:
             p.f[:] = f

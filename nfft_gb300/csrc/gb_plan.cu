@@ -36,6 +36,11 @@ template <> struct Api<double> {
   static void *mal(size_t n) { return nfft_malloc(n); }
   static void fre(void *p) { nfft_free(p); }
   static const cufftType fft_type = CUFFT_Z2Z;
+  static void set_mv(plan *p)
+  {
+    p->mv_trafo = (void (*)(void *))nfft_trafo;
+    p->mv_adjoint = (void (*)(void *))nfft_adjoint;
+  }
 };
 template <> struct Api<float> {
   typedef nfftf_plan plan;
@@ -43,6 +48,11 @@ template <> struct Api<float> {
   static void *mal(size_t n) { return nfftf_malloc(n); }
   static void fre(void *p) { nfftf_free(p); }
   static const cufftType fft_type = CUFFT_C2C;
+  static void set_mv(plan *p)
+  {
+    p->mv_trafo = (void (*)(void *))nfftf_trafo;
+    p->mv_adjoint = (void (*)(void *))nfftf_adjoint;
+  }
 };
 
 static void check_fft(cufftResult r, const char *what)
@@ -260,6 +270,7 @@ static void init_help(typename Api<R>::plan *ths)
                      ? (NFFT_INT *)Api<R>::mal(sizeof(NFFT_INT) * 2U * (size_t)ths->M_total)
                      : nullptr;
   ths->MEASURE_TIME_t[0] = ths->MEASURE_TIME_t[1] = ths->MEASURE_TIME_t[2] = 0;
+  Api<R>::set_mv(ths);  // nfft.c:6044-6045
 
   Ctx<R> *c = new Ctx<R>();
   Geom<R> &g = c->g;

@@ -493,6 +493,7 @@ static void host_before_loop(typename SApi<R>::splan *ths)
   const unsigned fl = ths->flags;
   const R *w = (fl & PRECOMPUTE_WEIGHT) ? ths->w : nullptr;
   const R *wh = (fl & PRECOMPUTE_DAMP) ? ths->w_hat : nullptr;
+  if (!mv || !mv->mv_trafo || !mv->mv_adjoint) fatal("solver: mv plan without mv_trafo / mv_adjoint");
   H::wcp((R *)mv->f_hat, nullptr, (R *)ths->f_hat_iter, N);
   std::swap(ths->r_iter, mv->f);
   mv->mv_trafo(mv);

@@ -1,0 +1,114 @@
+// gb_b3group.cu -- instantiations and launchers of the 3-D sub-cell group
+// kernels (see gb_b3group.cuh).
+#include <type_traits>
+
+#include "gb_b3group.cuh"
+
+namespace gb {
+
+static constexpr int G3_CS = 2;  // sub-cell edge
+
+template <typename R, int W>
+static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<R>::T *grid,
+                   const R *xs, const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g,
+                   cudaStream_t s)
+{
+  static bool attr = false;
+  const size_t smem = g3_smem_bytes<R, W, G3_CS>(g);
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(k_b3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    GB_CUDA(cudaFuncSetAttribute(k_bt3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    attr = true;
+  }
+  if (adjoint) {
+    k_bt3_group<R, W, G3_CS><<<nitems, G3_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
+    GB_LAUNCHED("bt3_group");
+  } else {
+    k_b3_group<R, W, G3_CS><<<nitems, G3_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
+    GB_LAUNCHED("b3_group");
+  }
+}
+
+template <typename R> struct G3Set;
+template <> struct G3Set<float> {
+  static bool has(int w) { return w == 8 || w == 10 || w == 14; }
+  static size_t smem(const Geom<float> &g)
+  {
+    switch (g.w) {
+      case 8: return g3_smem_bytes<float, 8, G3_CS>(g);
+      case 10: return g3_smem_bytes<float, 10, G3_CS>(g);
+      case 14: return g3_smem_bytes<float, 14, G3_CS>(g);
+    }
+    return 0;
+  }
+  static void run(bool adj, const WorkItem *it, int ni, float2 *grid, const float *xs, const uint32_t *perm,
+                  float2 *f, const Geom<float> &g, cudaStream_t s)
+  {
+    switch (g.w) {
+      case 8: run_g3<float, 8>(adj, it, ni, grid, xs, perm, f, g, s); return;
+      case 10: run_g3<float, 10>(adj, it, ni, grid, xs, perm, f, g, s); return;
+      case 14: run_g3<float, 14>(adj, it, ni, grid, xs, perm, f, g, s); return;
+    }
+    fatal("no 3-D group kernel for w=%d", g.w);
+  }
+};
+template <> struct G3Set<double> {
+  static bool has(int w) { return w == 10 || w == 14; }
+  static size_t smem(const Geom<double> &g)
+  {
+    switch (g.w) {
+      case 10: return g3_smem_bytes<double, 10, G3_CS>(g);
+      case 14: return g3_smem_bytes<double, 14, G3_CS>(g);
+    }
+    return 0;
+  }
+  static void run(bool adj, const WorkItem *it, int ni, double2 *grid, const double *xs,
+                  const uint32_t *perm, double2 *f, const Geom<double> &g, cudaStream_t s)
+  {
+    switch (g.w) {
+      case 10: run_g3<double, 10>(adj, it, ni, grid, xs, perm, f, g, s); return;
+      case 14: run_g3<double, 14>(adj, it, ni, grid, xs, perm, f, g, s); return;
+    }
+    fatal("no 3-D group kernel for w=%d", g.w);
+  }
+};
+
+template <typename R>
+bool group3_supported(int w) { return G3Set<R>::has(w); }
+template <typename R>
+size_t group3_smem_bytes(const Geom<R> &g) { return G3Set<R>::smem(g); }
+int group3_subcell_edge() { return G3_CS; }
+int group3_max_item() { return G3_MAXITEM; }
+
+template <typename R>
+void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
+                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+{
+  if (nitems > 0)
+    G3Set<R>::run(false, items, nitems, const_cast<typename Cx<R>::T *>(grid), xs, perm, f, g, s);
+}
+
+template <typename R>
+void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
+                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+{
+  if (nitems > 0)
+    G3Set<R>::run(true, items, nitems, grid, xs, perm, const_cast<typename Cx<R>::T *>(f), g, s);
+}
+
+template bool group3_supported<float>(int);
+template bool group3_supported<double>(int);
+template size_t group3_smem_bytes<float>(const Geom<float> &);
+template size_t group3_smem_bytes<double>(const Geom<double> &);
+template void launch_b3_group<float>(const WorkItem *, int, const float2 *, const float *, const uint32_t *,
+                                     float2 *, const Geom<float> &, cudaStream_t);
+template void launch_b3_group<double>(const WorkItem *, int, const double2 *, const double *,
+                                      const uint32_t *, double2 *, const Geom<double> &, cudaStream_t);
+template void launch_bt3_group<float>(const WorkItem *, int, float2 *, const float *, const uint32_t *,
+                                      const float2 *, const Geom<float> &, cudaStream_t);
+template void launch_bt3_group<double>(const WorkItem *, int, double2 *, const double *, const uint32_t *,
+                                       const double2 *, const Geom<double> &, cudaStream_t);
+
+}  // namespace gb

@@ -50,6 +50,8 @@ struct Geom {
   int T[GB_MAXD];        // tile edge per dim
   int ntile[GB_MAXD];    // tiles per dim (n_t / T_t, rounded up)
   int ext[GB_MAXD];      // padded subgrid edge T_t + w - 1
+  int cs;                // sub-cell edge of the 3-D group kernels (1 = off)
+  int sub;               // sub-cells per tile ((T/cs)^d, 1 = off)
 };
 
 struct WorkItem {

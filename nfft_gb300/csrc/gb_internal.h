@@ -30,8 +30,9 @@ void launch_node_keys(const R *x, const Geom<R> &g, uint32_t *tile_key, uint32_t
                       uint32_t *idx, cudaStream_t s);
 template <typename R>
 void launch_gather_x(const R *x, const uint32_t *perm, R *xs, const Geom<R> &g, cudaStream_t s);
-void launch_tile_starts(const uint32_t *sorted_keys, long long M, int ntiles, uint32_t *start,
-                        cudaStream_t s);
+// start[t] = first sorted position whose key / div >= t, t in [0, ntiles]
+void launch_tile_starts(const uint32_t *sorted_keys, long long M, int ntiles, uint32_t div,
+                        uint32_t *start, cudaStream_t s);
 // fills items (capacity >= ntiles + M/chunk + 1); returns the item count
 // (synchronises the stream once)
 int build_work_items(const uint32_t *start, int ntiles, int chunk, WorkItem *items,
@@ -64,6 +65,19 @@ template <typename R>
 void launch_bt_tiled(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g,
                      cudaStream_t s);
+// 3-D sub-cell group kernels (fast path of the 3-D transform)
+template <typename R>
+bool group3_supported(int w);
+template <typename R>
+size_t group3_smem_bytes(const Geom<R> &g);
+int group3_subcell_edge();
+int group3_max_item();
+template <typename R>
+void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
+                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
+template <typename R>
+void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
+                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
 // generic global-memory kernels for any d and m
 template <typename R>
 void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,

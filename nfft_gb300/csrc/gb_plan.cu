@@ -68,6 +68,7 @@ struct Ctx {
   unsigned flags = 0;
   bool direct = false;   // reference switches to the NDFT (nfft.c:5658-5665)
   bool tiled = false;
+  bool group3 = false;  // 3-D sub-cell group kernels
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // FFT: one plan for d <= 3; for d > 3 a rank-3 plan over the last three
@@ -144,6 +145,22 @@ static void choose_tiles(Ctx<R> *c)
     c->tiled = T > 0;
   }
   if (!c->tiled) T = g.d == 1 ? 256 : (g.d == 2 ? 32 : 8);  // binning only, for locality
+  // 3-D: sub-cell group kernels on 8^3 tiles where the grid allows
+  const int cs = group3_subcell_edge();
+  c->group3 = false;
+  g.cs = 1;
+  g.sub = 1;
+  if (g.d == 3 && group3_supported<R>(g.w) && g.n[0] >= 8 && g.n[1] >= 8 && g.n[2] >= 8) {
+    Geom<R> h = g;
+    for (int t = 0; t < 3; ++t) h.ext[t] = 8 + g.w - 1;
+    if (group3_smem_bytes<R>(h) <= 200 * 1024) {
+      c->group3 = true;
+      c->tiled = true;
+      T = 8;
+      g.cs = cs;
+      g.sub = (8 / cs) * (8 / cs) * (8 / cs);
+    }
+  }
   c->ntiles = 1;
   for (int t = 0; t < g.d; ++t) {
     g.T[t] = std::min(T, g.n[t]);
@@ -376,10 +393,11 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
   }
   if (!c->direct) {
     // tile order used by the transform kernels
-    radix_sort_pairs(k1, v1, k2, v2, (size_t)M, std::max(ceil_log2(c->ntiles), 1), temp, s);
+    radix_sort_pairs(k1, v1, k2, v2, (size_t)M, std::max(ceil_log2((long long)c->ntiles * g.sub), 1),
+                     temp, s);
     GB_CUDA(cudaMemcpyAsync(c->perm, v1, Mz * 4, cudaMemcpyDeviceToDevice, s));
     launch_gather_x<R>(c->x_dev, c->perm, c->xs, g, s);
-    launch_tile_starts(k1, M, c->ntiles, c->tile_start, s);
+    launch_tile_starts(k1, M, c->ntiles, (uint32_t)g.sub, c->tile_start, s);
     uint32_t *cnt = k2, *off = v2;  // reuse (>= ntiles entries needed)
     uint32_t *total;
     dev_alloc<R>((void **)&total, 16);
@@ -440,7 +458,8 @@ static void ensure_nodes(typename Api<R>::plan *ths, Ctx<R> *c)
 template <typename R>
 static void b_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
-  if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  else if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_b_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
 
@@ -459,7 +478,8 @@ static void bt_stage(Ctx<R> *c, const typename Cx<R>::T *f, cudaEvent_t *E)
 {
   GB_CUDA(cudaMemsetAsync(c->grid, 0, (size_t)c->g.n_total * sizeof(typename Cx<R>::T), c->stream));
   GB_CUDA(cudaEventRecord(E[6], c->stream));
-  if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  else if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_bt_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
 

@@ -238,17 +238,20 @@ __global__ void k_node_keys(const R *__restrict__ x, Geom<R> g, uint32_t *__rest
 {
   const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= g.M) return;
-  uint32_t tk = 0, rk = 0;
+  uint32_t tk = 0, rk = 0, sk = 0;
   for (int t = 0; t < g.d; ++t) {
     const R xt = x[j * g.d + t];
     const int u = wrap(node_u<R>(xt, g.nR[t], g.m), g.n[t]);
-    tk = tk * (uint32_t)g.ntile[t] + (uint32_t)(u / g.T[t]);
+    const int tile = u / g.T[t];
+    tk = tk * (uint32_t)g.ntile[t] + (uint32_t)tile;
+    // sub-cell of the window start inside its tile (group kernels)
+    sk = sk * (uint32_t)(g.T[t] / g.cs) + (uint32_t)((u - tile * g.T[t]) / g.cs);
     // reference sort key: floor(n*x - m) in plan precision, no contraction
     const int help = (int)gb_floor(sub_rn(mul_rn(g.nR[t], xt), (R)g.m));
     const int ut = ((help % g.n[t]) + g.n[t]) % g.n[t];
     rk = rk * (uint32_t)g.n[t] + (uint32_t)ut;
   }
-  tile_key[j] = tk;
+  tile_key[j] = g.sub > 1 ? tk * (uint32_t)g.sub + sk : tk;
   if (ref_key) ref_key[j] = rk;
   idx[j] = (uint32_t)j;
 }
@@ -285,20 +288,20 @@ void launch_gather_x(const R *x, const uint32_t *perm, R *xs, const Geom<R> &g, 
 
 // start[t] = first sorted position with key >= t, for t in [0, ntiles]
 __global__ void k_tile_starts(const uint32_t *__restrict__ key, long long M, int ntiles,
-                              uint32_t *__restrict__ start)
+                              uint32_t div, uint32_t *__restrict__ start)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i > M) return;
-  const long long lo = (i == 0) ? -1 : (long long)key[i - 1];
-  const long long hi = (i == M) ? (long long)ntiles : (long long)key[i];
+  const long long lo = (i == 0) ? -1 : (long long)(key[i - 1] / div);
+  const long long hi = (i == M) ? (long long)ntiles : (long long)(key[i] / div);
   for (long long t = lo + 1; t <= hi; ++t) start[t] = (uint32_t)i;
 }
 
-void launch_tile_starts(const uint32_t *sorted_keys, long long M, int ntiles, uint32_t *start,
-                        cudaStream_t s)
+void launch_tile_starts(const uint32_t *sorted_keys, long long M, int ntiles, uint32_t div,
+                        uint32_t *start, cudaStream_t s)
 {
   const int th = 256;
-  k_tile_starts<<<(unsigned)((M + 1 + th - 1) / th), th, 0, s>>>(sorted_keys, M, ntiles, start);
+  k_tile_starts<<<(unsigned)((M + 1 + th - 1) / th), th, 0, s>>>(sorted_keys, M, ntiles, div, start);
   GB_LAUNCHED("tile_starts");
 }
 

@@ -7,22 +7,26 @@
 //
 // Node set-up sorts the nodes by (tile, sub-cell): a tile is T^3 cells of the
 // oversampled grid, a sub-cell CS^3 cells of a tile.  All nodes whose window
-// start lies in one sub-cell share one box of (w + CS - 1)^3 grid cells.  A
-// warp treats such a group of nodes together:
+// start lies in one sub-cell share one box of (w + CS - 1)^3 grid cells.
+//
+// A CTA takes one work item (a tile and a range of its nodes) and stages the
+// tile's padded subgrid ((T + w - 1)^3 cells, wrapped periodically) in shared
+// memory as separate real and imaginary planes; rows are ext_z apart (odd),
+// so the row accesses of a warp hit distinct banks.  The item's nodes are cut
+// into units of at most PMAX nodes of one sub-cell; the warps take units in
+// turn:
+//  * all 32 lanes evaluate the unit's Kaiser-Bessel window values on the fly
+//    (3 (2m+2) per node) into zero-padded box vectors in shared memory;
 //  * the lanes own the (x, y) rows of the box and hold a row's w + CS - 1
 //    values along z in registers;
-//  * each node's window is evaluated once, on the fly, into three
-//    zero-padded vectors in shared memory, read back as broadcasts;
-//  * B   contracts z by FMAs in registers, then x and y, and reduces the
-//        per-lane partial sums of up to PMAX nodes with one butterfly
-//        transpose-reduction over the warp;
-//  * B^T builds the rank-1 tensor products of up to PMAX nodes in registers
-//        and adds each row to the shared subgrid once per pass (instead of
-//        once per tap and node).
-// The tile's padded subgrid ((T + w - 1)^3 cells, wrapped periodically) sits
-// in shared memory as separate real and imaginary planes; rows are ext_z
-// apart (odd), so the row accesses of a warp hit distinct banks.
+//  * B   contracts z by FMAs, then x and y, and reduces the per-lane partial
+//        sums of the unit's nodes with one butterfly transpose-reduction;
+//  * B^T builds the rank-1 tensor products of the unit's nodes in registers
+//        and adds each row to the shared subgrid once per unit (not once per
+//        tap and node); the subgrid goes to the global grid once per item.
 #pragma once
+
+#include <type_traits>
 
 #include "gb_internal.h"
 
@@ -30,17 +34,19 @@ namespace gb {
 
 static constexpr int G3_THREADS = 256;
 static constexpr int G3_WARPS = G3_THREADS / 32;
-static constexpr int G3_MAXITEM = 1024;  // nodes per work item (node set-up chunk)
+static constexpr int G3_WINDOW = 1024;     // nodes per unit-building window
+static constexpr int G3_MAXITEM = 16384;   // nodes per work item
 
 template <typename R, int W, int CS>
 struct G3 {
-  static constexpr int BOX = W + CS - 1;                        // box edge
-  static constexpr int BOXP = (BOX + 3) / 4 * 4;                // padded for vector loads
-  static constexpr int ROWS = BOX * BOX;                        // (x, y) rows of a box
-  static constexpr int RITER = (ROWS + 31) / 32;                // row iterations per lane
-  static constexpr int PMAX = sizeof(R) == 4 ? 16 : 8;          // nodes per pass
-  static constexpr int NV = 2 * PMAX;                           // reduced values per pass
+  static constexpr int BOX = W + CS - 1;                          // box edge
+  static constexpr int BOXP = (BOX + 3) / 4 * 4;                  // padded for vector loads
+  static constexpr int ROWS = BOX * BOX;                          // (x, y) rows of a box
+  static constexpr int RITER = (ROWS + 31) / 32;                  // row iterations per lane
+  static constexpr int PMAX = sizeof(R) == 4 ? 16 : 8;            // nodes per unit
+  static constexpr int NV = 2 * PMAX;                             // reduced values per unit
   static constexpr int WARP_FLOATS = 3 * PMAX * BOXP + 2 * PMAX;  // per-warp scratch (R)
+  static constexpr int INTS = 4 * G3_WINDOW + 2 + G3_WARPS;       // sub, gstart, ucount, ustart, wsum
 };
 
 template <typename R, int W, int CS>
@@ -48,8 +54,7 @@ inline size_t g3_smem_bytes(const Geom<R> &g)
 {
   typedef G3<R, W, CS> P;
   const size_t cells = (size_t)g.ext[0] * g.ext[1] * g.ext[2];
-  return (2 * cells + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) +
-         (2 * G3_MAXITEM + 1 + G3_WARPS) * sizeof(int);
+  return (2 * cells + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
 }
 
 // Butterfly transpose-reduction over the warp: NV values per lane in; lane l
@@ -75,7 +80,7 @@ __device__ __forceinline__ void warp_transpose_reduce(R (&v)[NV])
 }
 
 // sub-cell of a node inside its tile (row-major over the tile's sub-cells);
-// loc = window start relative to the tile origin, box0 = its sub-cell origin
+// box0 = origin of that sub-cell relative to the tile origin
 template <typename R, int CS>
 __device__ __forceinline__ int node_subcell(const R *x3, const Geom<R> &g, const int *org, int *box0)
 {
@@ -91,63 +96,111 @@ __device__ __forceinline__ int node_subcell(const R *x3, const Geom<R> &g, const
   return s;
 }
 
-// Group discovery inside one work item: gstart[k] = first node of the k-th
-// run of equal sub-cell ids (in sorted order), gstart[ng] = item end.
-template <typename R, int CS>
-__device__ int g3_groups(const WorkItem &it, const R *__restrict__ xs, const Geom<R> &g,
-                         const int *org, int *sub, int *gstart, int *wsum)
+// Exclusive scan of n <= 4 * G3_THREADS ints in place; returns the total.
+__device__ __forceinline__ int g3_block_scan(int *a, int n, int *wsum)
 {
-  const int n = it.end - it.start;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = threadIdx.x * 4;
+  int v[4], s = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[i] = (b + i < n) ? a[b + i] : 0;
+    s += v[i];
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  int before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < G3_WARPS; ++w) {
+    if (w < warp) before += wsum[w];
+    total += wsum[w];
+  }
+  int run = before + incl - s;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (b + i < n) a[b + i] = run;
+    run += v[i];
+  }
+  __syncthreads();
+  return total;
+}
+
+// Units of one window [c0, c1) of sorted nodes: runs of equal sub-cell cut
+// into pieces of at most PMAX nodes.  ustart[0..nu] (ustart[nu] = c1).
+template <typename R, int CS, int PMAX>
+__device__ int g3_units(int c0, int c1, const R *__restrict__ xs, const Geom<R> &g, const int *org,
+                        int *sub, int *gstart, int *ucnt, int *ustart, int *wsum)
+{
+  const int n = c1 - c0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int k = threadIdx.x; k < n; k += G3_THREADS) {
     int b[3];
-    sub[k] = node_subcell<R, CS>(xs + (long long)(it.start + k) * 3, g, org, b);
+    sub[k] = node_subcell<R, CS>(xs + (long long)(c0 + k) * 3, g, org, b);
   }
   __syncthreads();
-  int base = 0;
-  for (int c0 = 0; c0 < n; c0 += G3_THREADS) {
-    const int k = c0 + threadIdx.x;
+  // ordered compaction of the run heads
+  int ng = 0;
+  for (int k0 = 0; k0 < n; k0 += G3_THREADS) {
+    const int k = k0 + threadIdx.x;
     const bool head = k < n && (k == 0 || sub[k] != sub[k - 1]);
     const unsigned bal = __ballot_sync(0xffffffffu, head);
     if (lane == 0) wsum[warp] = __popc(bal);
     __syncthreads();
-    int before = base, total = 0;
+    int before = ng, total = 0;
 #pragma unroll
     for (int w = 0; w < G3_WARPS; ++w) {
       if (w < warp) before += wsum[w];
       total += wsum[w];
     }
-    if (head) gstart[before + __popc(bal & ((1u << lane) - 1u))] = it.start + k;
-    base += total;
+    if (head) gstart[before + __popc(bal & ((1u << lane) - 1u))] = k;
+    ng += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0) gstart[base] = it.end;
+  if (threadIdx.x == 0) gstart[ng] = n;
   __syncthreads();
-  return base;
+  for (int k = threadIdx.x; k < ng; k += G3_THREADS)
+    ucnt[k] = (gstart[k + 1] - gstart[k] + PMAX - 1) / PMAX;
+  __syncthreads();
+  const int nu = g3_block_scan(ucnt, ng, wsum);
+  for (int k = threadIdx.x; k < ng; k += G3_THREADS) {
+    const int s0 = gstart[k], s1 = gstart[k + 1];
+    int u = ucnt[k];
+    for (int p = s0; p < s1; p += PMAX) ustart[u++] = c0 + p;
+  }
+  if (threadIdx.x == 0) ustart[nu] = c1;
+  __syncthreads();
+  return nu;
 }
 
-// Window values of node i, zero-padded into the warp's box vectors.
+// All 32 lanes evaluate the window values of the unit's np nodes into the
+// warp's zero-padded box vectors wx, wy, wz ([PMAX][BOXP] each).
 template <typename R, int W, int CS>
-__device__ __forceinline__ void g3_node_weights(long long i, const R *__restrict__ xs, const Geom<R> &g,
-                                                const int *org, const int *box0, R *wx, R *wy, R *wz)
+__device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restrict__ xs, const Geom<R> &g,
+                                                const int *org, const int *box0, R *wx)
 {
   typedef G3<R, W, CS> P;
-  R *dst[3] = {wx, wy, wz};
-#pragma unroll
-  for (int t = 0; t < 3; ++t) {
-    const R x = xs[i * 3 + t];
+  const int lane = threadIdx.x & 31;
+  const int nz = 3 * P::PMAX * P::BOXP;
+  for (int k = lane; k < nz; k += 32) wx[k] = R(0);
+  __syncwarp();
+  for (int k = lane; k < np * 3 * W; k += 32) {
+    const int j = k / (3 * W), rem = k - j * (3 * W);
+    const int t = rem / W, l = rem - t * W;
+    const R x = xs[(long long)(u0 + j) * 3 + t];
     const int u = node_u<R>(x, g.nR[t], g.m);
     const int o = wrap(u, g.n[t]) - org[t] - box0[t];  // in [0, CS)
-    R psi[W];
-    node_psi<R, W>(x, u, g.nR[t], g.mm, g.b[t], psi);
-#pragma unroll
-    for (int b = 0; b < P::BOXP; ++b) dst[t][b] = R(0);
-#pragma unroll
-    for (int q = 0; q < W; ++q) dst[t][o + q] = psi[q];
+    wx[(t * P::PMAX + j) * P::BOXP + o + l] = kb_phi<R>(x - R(u + l) / g.nR[t], g.nR[t], g.mm, g.b[t]);
   }
+  __syncwarp();
 }
 
-template <typename R, int W, int CS>
+template <typename R>
 __device__ __forceinline__ void g3_tile_origin(const WorkItem &it, const Geom<R> &g, int *org)
 {
   int rem = it.tile;
@@ -170,6 +223,40 @@ __device__ __forceinline__ long long g3_global_cell(int idx, const int *org, con
   return ((long long)p0 * g.n[1] + p1) * g.n[2] + p2;
 }
 
+// load the padded z-vector of a node's box (BOXP reals) from shared memory
+template <typename R, int BOXP>
+__device__ __forceinline__ void g3_load_vec(const R *src, R (&dst)[BOXP])
+{
+  typedef typename std::conditional<sizeof(R) == 4, float4, double2>::type V;
+  constexpr int VPER = sizeof(V) / sizeof(R);
+  const V *v = reinterpret_cast<const V *>(src);
+#pragma unroll
+  for (int q = 0; q < BOXP / VPER; ++q) {
+    const V t = v[q];
+    const R *tt = reinterpret_cast<const R *>(&t);
+#pragma unroll
+    for (int e = 0; e < VPER; ++e) dst[q * VPER + e] = tt[e];
+  }
+}
+
+struct G3Smem {
+  template <typename R, int W, int CS>
+  __device__ static void carve(unsigned char *raw, int cells, R *&wscratch, R *&sre, R *&sim, int *&sub,
+                               int *&gstart, int *&ucnt, int *&ustart, int *&wsum)
+  {
+    typedef G3<R, W, CS> P;
+    R *base = reinterpret_cast<R *>(raw);  // per-warp scratch first: 16-byte aligned
+    wscratch = base + (threadIdx.x >> 5) * P::WARP_FLOATS;
+    sre = base + G3_WARPS * P::WARP_FLOATS;
+    sim = sre + cells;
+    sub = reinterpret_cast<int *>(sim + cells);
+    gstart = sub + G3_WINDOW;
+    ucnt = gstart + G3_WINDOW + 1;
+    ustart = ucnt + G3_WINDOW;
+    wsum = ustart + G3_WINDOW + 1;
+  }
+};
+
 template <typename R, int W, int CS>
 __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__restrict__ items,
                                                              const typename Cx<R>::T *__restrict__ grid,
@@ -179,42 +266,32 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
 {
   typedef G3<R, W, CS> P;
   typedef typename Cx<R>::T C;
-  typedef typename std::conditional<sizeof(R) == 4, float4, double2>::type V4;
-  constexpr int VPER = sizeof(V4) / sizeof(R);  // reals per vector load
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cells = g.ext[0] * g.ext[1] * g.ext[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  R *wbase = reinterpret_cast<R *>(smem_raw);  // per-warp scratch first: 16-byte aligned
-  R *wx = wbase + warp * P::WARP_FLOATS;
+  R *wx, *sre, *sim;
+  int *sub, *gstart, *ucnt, *ustart, *wsum;
+  G3Smem::carve<R, W, CS>(smem_raw, cells, wx, sre, sim, sub, gstart, ucnt, ustart, wsum);
   R *wy = wx + P::PMAX * P::BOXP;
   R *wz = wy + P::PMAX * P::BOXP;
-  R *sre = wbase + G3_WARPS * P::WARP_FLOATS;
-  R *sim = sre + cells;
-  int *sub = reinterpret_cast<int *>(sim + cells);
-  int *gstart = sub + G3_MAXITEM;
-  int *wsum = gstart + G3_MAXITEM + 1;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
-  g3_tile_origin<R, W, CS>(it, g, org);
+  g3_tile_origin<R>(it, g, org);
   for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
     const C v = grid[g3_global_cell<R>(idx, org, g)];
     sre[idx] = v.x;
     sim[idx] = v.y;
   }
-  const int ng = g3_groups<R, CS>(it, xs, g, org, sub, gstart, wsum);  // has barriers
   const int e1 = g.ext[1], e2 = g.ext[2];
-
-  for (int gi = warp; gi < ng; gi += G3_WARPS) {
-    const int g0 = gstart[gi], g1 = gstart[gi + 1];
-    int box0[3];
-    node_subcell<R, CS>(xs + (long long)g0 * 3, g, org, box0);
-    for (int p0 = g0; p0 < g1; p0 += P::PMAX) {
-      const int np = min(P::PMAX, g1 - p0);
-      if (lane < np)
-        g3_node_weights<R, W, CS>(p0 + lane, xs, g, org, box0, wx + lane * P::BOXP,
-                                  wy + lane * P::BOXP, wz + lane * P::BOXP);
-      __syncwarp();
+  for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
+    const int c1 = min(c0 + G3_WINDOW, it.end);
+    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, sub, gstart, ucnt, ustart, wsum);
+    for (int ui = warp; ui < nu; ui += G3_WARPS) {
+      const int u0 = ustart[ui], np = ustart[ui + 1] - u0;
+      int box0[3];
+      node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
+      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, wx);
       R acc[P::NV];
 #pragma unroll
       for (int j = 0; j < P::NV; ++j) acc[j] = R(0);
@@ -234,14 +311,7 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
           for (int j = 0; j < P::PMAX; ++j) {
             if (j < np) {
               R wzj[P::BOXP];
-              const V4 *wv = reinterpret_cast<const V4 *>(wz + j * P::BOXP);
-#pragma unroll
-              for (int q = 0; q < P::BOXP / VPER; ++q) {
-                const V4 t = wv[q];
-                const R *tt = reinterpret_cast<const R *>(&t);
-#pragma unroll
-                for (int e = 0; e < VPER; ++e) wzj[q * VPER + e] = tt[e];
-              }
+              g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
               R tr = R(0), ti = R(0);
 #pragma unroll
               for (int z = 0; z < P::BOX; ++z) {
@@ -258,9 +328,10 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
       warp_transpose_reduce<R, P::NV>(acc);
       const R re = __shfl_sync(0xffffffffu, acc[0], (2 * lane) & 31);
       const R im = __shfl_sync(0xffffffffu, acc[0], (2 * lane + 1) & 31);
-      if (lane < np) f[perm[p0 + lane]] = cmake(re, im);
+      if (lane < np) f[perm[u0 + lane]] = cmake(re, im);
       __syncwarp();
     }
+    __syncthreads();
   }
 }
 
@@ -274,46 +345,37 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
 {
   typedef G3<R, W, CS> P;
   typedef typename Cx<R>::T C;
-  typedef typename std::conditional<sizeof(R) == 4, float4, double2>::type V4;
-  constexpr int VPER = sizeof(V4) / sizeof(R);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cells = g.ext[0] * g.ext[1] * g.ext[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  R *wbase = reinterpret_cast<R *>(smem_raw);
-  R *wx = wbase + warp * P::WARP_FLOATS;
+  R *wx, *sre, *sim;
+  int *sub, *gstart, *ucnt, *ustart, *wsum;
+  G3Smem::carve<R, W, CS>(smem_raw, cells, wx, sre, sim, sub, gstart, ucnt, ustart, wsum);
   R *wy = wx + P::PMAX * P::BOXP;
   R *wz = wy + P::PMAX * P::BOXP;
   R *fv = wz + P::PMAX * P::BOXP;
-  R *sre = wbase + G3_WARPS * P::WARP_FLOATS;
-  R *sim = sre + cells;
-  int *sub = reinterpret_cast<int *>(sim + cells);
-  int *gstart = sub + G3_MAXITEM;
-  int *wsum = gstart + G3_MAXITEM + 1;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
-  g3_tile_origin<R, W, CS>(it, g, org);
+  g3_tile_origin<R>(it, g, org);
   for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
     sre[idx] = R(0);
     sim[idx] = R(0);
   }
-  const int ng = g3_groups<R, CS>(it, xs, g, org, sub, gstart, wsum);
   const int e1 = g.ext[1], e2 = g.ext[2];
-
-  for (int gi = warp; gi < ng; gi += G3_WARPS) {
-    const int g0 = gstart[gi], g1 = gstart[gi + 1];
-    int box0[3];
-    node_subcell<R, CS>(xs + (long long)g0 * 3, g, org, box0);
-    for (int p0 = g0; p0 < g1; p0 += P::PMAX) {
-      const int np = min(P::PMAX, g1 - p0);
+  for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
+    const int c1 = min(c0 + G3_WINDOW, it.end);
+    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, sub, gstart, ucnt, ustart, wsum);
+    for (int ui = warp; ui < nu; ui += G3_WARPS) {
+      const int u0 = ustart[ui], np = ustart[ui + 1] - u0;
+      int box0[3];
+      node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
       if (lane < np) {
-        g3_node_weights<R, W, CS>(p0 + lane, xs, g, org, box0, wx + lane * P::BOXP,
-                                  wy + lane * P::BOXP, wz + lane * P::BOXP);
-        const C v = f[perm[p0 + lane]];
+        const C v = f[perm[u0 + lane]];
         fv[2 * lane] = v.x;
         fv[2 * lane + 1] = v.y;
       }
-      __syncwarp();
+      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, wx);  // ends with __syncwarp
 #pragma unroll 1
       for (int ri = 0; ri < P::RITER; ++ri) {
         const int row = lane + 32 * ri;
@@ -328,14 +390,7 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
               const R wxy = wx[j * P::BOXP + bx] * wy[j * P::BOXP + by];
               const R hr = wxy * fv[2 * j], hi = wxy * fv[2 * j + 1];
               R wzj[P::BOXP];
-              const V4 *wv = reinterpret_cast<const V4 *>(wz + j * P::BOXP);
-#pragma unroll
-              for (int q = 0; q < P::BOXP / VPER; ++q) {
-                const V4 t = wv[q];
-                const R *tt = reinterpret_cast<const R *>(&t);
-#pragma unroll
-                for (int e = 0; e < VPER; ++e) wzj[q * VPER + e] = tt[e];
-              }
+              g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
 #pragma unroll
               for (int z = 0; z < P::BOX; ++z) {
                 ar[z] += wzj[z] * hr;
@@ -353,8 +408,8 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
       }
       __syncwarp();
     }
+    __syncthreads();
   }
-  __syncthreads();
   // one vector reduction per non-zero cell of the padded subgrid
   for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
     const R vr = sre[idx], vi = sim[idx];

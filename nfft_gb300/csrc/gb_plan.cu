@@ -405,7 +405,8 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
       dev_alloc<R>((void **)&cnt, (size_t)c->ntiles * 4);
       dev_alloc<R>((void **)&off, (size_t)c->ntiles * 4);
     }
-    c->nitems = c->tiled ? build_work_items(c->tile_start, c->ntiles, 1024, c->items, cnt, off,
+    const int chunk = c->group3 ? group3_max_item() : 1024;
+    c->nitems = c->tiled ? build_work_items(c->tile_start, c->ntiles, chunk, c->items, cnt, off,
                                             total, temp, s)
                          : 0;
     if (cnt != k2) {

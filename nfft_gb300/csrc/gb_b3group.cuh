@@ -5,16 +5,16 @@
 // (nfft.c:4020-4265), and nfft_adjoint_3d_B (nfft.c:5126-5384) with its
 // blockwise scatter (nfft.c:4289-4388).
 //
-// Node set-up sorts the nodes by (tile, sub-cell): a tile is T^3 cells of the
+// Node set-up sorts the nodes by (tile, sub-cell): a tile is 8^3 cells of the
 // oversampled grid, a sub-cell CS^3 cells of a tile.  All nodes whose window
 // start lies in one sub-cell share one box of (w + CS - 1)^3 grid cells.
 //
 // A CTA takes one work item (a tile and a range of its nodes) and stages the
-// tile's padded subgrid ((T + w - 1)^3 cells, wrapped periodically) in shared
-// memory as separate real and imaginary planes; rows are ext_z apart (odd),
-// so the row accesses of a warp hit distinct banks.  The item's nodes are cut
-// into units of at most PMAX nodes of one sub-cell; the warps take units in
-// turn:
+// tile's padded subgrid ((8 + w - 1)^3 cells, wrapped periodically) in shared
+// memory as separate real and imaginary planes whose x / y strides are padded
+// so that the 32 box rows a warp reads at once fall in distinct banks.  The
+// item's nodes are cut into units of at most PMAX nodes of one sub-cell; the
+// warps take units in turn:
 //  * all 32 lanes evaluate the unit's Kaiser-Bessel window values on the fly
 //    (3 (2m+2) per node) into zero-padded box vectors in shared memory;
 //  * the lanes own the (x, y) rows of the box and hold a row's w + CS - 1
@@ -34,18 +34,22 @@ namespace gb {
 
 static constexpr int G3_THREADS = 256;
 static constexpr int G3_WARPS = G3_THREADS / 32;
+static constexpr int G3_TILE = 8;          // tile edge (cells)
 static constexpr int G3_WINDOW = 1024;     // nodes per unit-building window
 static constexpr int G3_MAXITEM = 16384;   // nodes per work item
 
 template <typename R, int W, int CS>
 struct G3 {
+  static constexpr int EXT = G3_TILE + W - 1;                     // padded subgrid edge
   static constexpr int BOX = W + CS - 1;                          // box edge
   static constexpr int BOXP = (BOX + 3) / 4 * 4;                  // padded for vector loads
   static constexpr int ROWS = BOX * BOX;                          // (x, y) rows of a box
   static constexpr int RITER = (ROWS + 31) / 32;                  // row iterations per lane
   static constexpr int PMAX = sizeof(R) == 4 ? 16 : 8;            // nodes per unit
   static constexpr int NV = 2 * PMAX;                             // reduced values per unit
-  static constexpr int WARP_FLOATS = 3 * PMAX * BOXP + 2 * PMAX;  // per-warp scratch (R)
+  // per-warp scratch (R): wx, wy, wz [PMAX][BOXP] each, f values [PMAX][2],
+  // window offsets t0 [3 PMAX], box offsets o [3 PMAX] (as int)
+  static constexpr int WARP_FLOATS = 3 * PMAX * BOXP + 2 * PMAX + 6 * PMAX;
   static constexpr int INTS = 4 * G3_WINDOW + 2 + G3_WARPS;       // sub, gstart, ucount, ustart, wsum
 };
 
@@ -53,8 +57,8 @@ template <typename R, int W, int CS>
 inline size_t g3_smem_bytes(const Geom<R> &g)
 {
   typedef G3<R, W, CS> P;
-  const size_t cells = (size_t)g.ext[0] * g.ext[1] * g.ext[2];
-  return (2 * cells + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
+  const size_t plane = (size_t)P::EXT * g.sx;
+  return (2 * plane + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
 }
 
 // Butterfly transpose-reduction over the warp: NV values per lane in; lane l
@@ -91,7 +95,7 @@ __device__ __forceinline__ int node_subcell(const R *x3, const Geom<R> &g, const
     const int loc = wrap(u, g.n[t]) - org[t];
     const int sc = loc / CS;
     box0[t] = sc * CS;
-    s = s * (g.T[t] / CS) + sc;
+    s = s * (G3_TILE / CS) + sc;
   }
   return s;
 }
@@ -179,23 +183,30 @@ __device__ int g3_units(int c0, int c1, const R *__restrict__ xs, const Geom<R> 
 }
 
 // All 32 lanes evaluate the window values of the unit's np nodes into the
-// warp's zero-padded box vectors wx, wy, wz ([PMAX][BOXP] each).
+// warp's zero-padded box vectors w[t][j][b] ([3][PMAX][BOXP]).  t0 / so are
+// per (node, dim) scratch: t0 = n x - u (the argument of tap 0), so = box
+// offset of the window.
 template <typename R, int W, int CS>
 __device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restrict__ xs, const Geom<R> &g,
-                                                const int *org, const int *box0, R *wx)
+                                                const int *org, const int *box0, R *w, R *t0, int *so)
 {
   typedef G3<R, W, CS> P;
   const int lane = threadIdx.x & 31;
-  const int nz = 3 * P::PMAX * P::BOXP;
-  for (int k = lane; k < nz; k += 32) wx[k] = R(0);
+  if (lane < 3 * np) {
+    const int j = lane / 3, t = lane - 3 * j;
+    const R xn = xs[(long long)(u0 + j) * 3 + t] * g.nR[t];
+    const int u = (int)gb_floor(xn) - g.m;  // node_u
+    so[lane] = wrap(u, g.n[t]) - org[t] - box0[t];
+    t0[lane] = xn - R(u);
+  }
   __syncwarp();
-  for (int k = lane; k < np * 3 * W; k += 32) {
-    const int j = k / (3 * W), rem = k - j * (3 * W);
-    const int t = rem / W, l = rem - t * W;
-    const R x = xs[(long long)(u0 + j) * 3 + t];
-    const int u = node_u<R>(x, g.nR[t], g.m);
-    const int o = wrap(u, g.n[t]) - org[t] - box0[t];  // in [0, CS)
-    wx[(t * P::PMAX + j) * P::BOXP + o + l] = kb_phi<R>(x - R(u + l) / g.nR[t], g.nR[t], g.mm, g.b[t]);
+  for (int k = lane; k < 3 * np * P::BOXP; k += 32) {
+    const int jt = k / P::BOXP, b = k - jt * P::BOXP;
+    const int j = jt / 3, t = jt - 3 * j;
+    const int l = b - so[jt];
+    R v = R(0);
+    if (l >= 0 && l < W) v = kb_window_t(t0[jt] - R(l), g.mm, g.b[t]);
+    w[(t * P::PMAX + j) * P::BOXP + b] = v;
   }
   __syncwarp();
 }
@@ -206,21 +217,23 @@ __device__ __forceinline__ void g3_tile_origin(const WorkItem &it, const Geom<R>
   int rem = it.tile;
 #pragma unroll
   for (int t = 2; t >= 0; --t) {
-    org[t] = (rem % g.ntile[t]) * g.T[t];
+    org[t] = (rem % g.ntile[t]) * G3_TILE;
     rem /= g.ntile[t];
   }
 }
 
-template <typename R>
-__device__ __forceinline__ long long g3_global_cell(int idx, const int *org, const Geom<R> &g)
+// subgrid cell idx (row-major over EXT^3) -> shared index and global index
+template <typename R, int EXT>
+__device__ __forceinline__ void g3_cell(int idx, const int *org, const Geom<R> &g, int &si, long long &gi)
 {
-  const int c2 = idx % g.ext[2], r = idx / g.ext[2];
-  const int c1 = r % g.ext[1], c0 = r / g.ext[1];
+  const int c2 = idx % EXT, r = idx / EXT;
+  const int c1 = r % EXT, c0 = r / EXT;
+  si = c0 * g.sx + c1 * g.sy + c2;
   int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
   p0 = p0 >= g.n[0] ? p0 - g.n[0] : p0;
   p1 = p1 >= g.n[1] ? p1 - g.n[1] : p1;
   p2 = p2 >= g.n[2] ? p2 - g.n[2] : p2;
-  return ((long long)p0 * g.n[1] + p1) * g.n[2] + p2;
+  gi = ((long long)p0 * g.n[1] + p1) * g.n[2] + p2;
 }
 
 // load the padded z-vector of a node's box (BOXP reals) from shared memory
@@ -239,17 +252,23 @@ __device__ __forceinline__ void g3_load_vec(const R *src, R (&dst)[BOXP])
   }
 }
 
+template <typename R, int W, int CS>
 struct G3Smem {
-  template <typename R, int W, int CS>
-  __device__ static void carve(unsigned char *raw, int cells, R *&wscratch, R *&sre, R *&sim, int *&sub,
-                               int *&gstart, int *&ucnt, int *&ustart, int *&wsum)
+  R *w, *fv, *t0;
+  int *so;
+  R *sre, *sim;
+  int *sub, *gstart, *ucnt, *ustart, *wsum;
+  __device__ G3Smem(unsigned char *raw, const Geom<R> &g)
   {
     typedef G3<R, W, CS> P;
     R *base = reinterpret_cast<R *>(raw);  // per-warp scratch first: 16-byte aligned
-    wscratch = base + (threadIdx.x >> 5) * P::WARP_FLOATS;
+    w = base + (threadIdx.x >> 5) * P::WARP_FLOATS;
+    fv = w + 3 * P::PMAX * P::BOXP;
+    t0 = fv + 2 * P::PMAX;
+    so = reinterpret_cast<int *>(t0 + 3 * P::PMAX);
     sre = base + G3_WARPS * P::WARP_FLOATS;
-    sim = sre + cells;
-    sub = reinterpret_cast<int *>(sim + cells);
+    sim = sre + P::EXT * g.sx;
+    sub = reinterpret_cast<int *>(sim + P::EXT * g.sx);
     gstart = sub + G3_WINDOW;
     ucnt = gstart + G3_WINDOW + 1;
     ustart = ucnt + G3_WINDOW;
@@ -267,31 +286,30 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
   typedef G3<R, W, CS> P;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int cells = g.ext[0] * g.ext[1] * g.ext[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  R *wx, *sre, *sim;
-  int *sub, *gstart, *ucnt, *ustart, *wsum;
-  G3Smem::carve<R, W, CS>(smem_raw, cells, wx, sre, sim, sub, gstart, ucnt, ustart, wsum);
-  R *wy = wx + P::PMAX * P::BOXP;
-  R *wz = wy + P::PMAX * P::BOXP;
+  G3Smem<R, W, CS> S(smem_raw, g);
+  const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
   g3_tile_origin<R>(it, g, org);
-  for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
-    const C v = grid[g3_global_cell<R>(idx, org, g)];
-    sre[idx] = v.x;
-    sim[idx] = v.y;
+  for (int idx = threadIdx.x; idx < P::EXT * P::EXT * P::EXT; idx += G3_THREADS) {
+    int si;
+    long long gi;
+    g3_cell<R, P::EXT>(idx, org, g, si, gi);
+    const C v = grid[gi];
+    S.sre[si] = v.x;
+    S.sim[si] = v.y;
   }
-  const int e1 = g.ext[1], e2 = g.ext[2];
   for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
     const int c1 = min(c0 + G3_WINDOW, it.end);
-    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, sub, gstart, ucnt, ustart, wsum);
+    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, S.sub, S.gstart, S.ucnt, S.ustart, S.wsum);
     for (int ui = warp; ui < nu; ui += G3_WARPS) {
-      const int u0 = ustart[ui], np = ustart[ui + 1] - u0;
+      const int u0 = S.ustart[ui], np = S.ustart[ui + 1] - u0;
       int box0[3];
       node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
-      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, wx);
+      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);
+      const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
       R acc[P::NV];
 #pragma unroll
       for (int j = 0; j < P::NV; ++j) acc[j] = R(0);
@@ -300,27 +318,33 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
         const int row = lane + 32 * ri;
         if (row < P::ROWS) {
           const int bx = row / P::BOX, by = row - bx * P::BOX;
-          const int base = ((box0[0] + bx) * e1 + (box0[1] + by)) * e2 + box0[2];
+          const int base = sbase + bx * g.sx + by * g.sy;
           R gr[P::BOX], gim[P::BOX];
 #pragma unroll
           for (int z = 0; z < P::BOX; ++z) {
-            gr[z] = sre[base + z];
-            gim[z] = sim[base + z];
+            gr[z] = S.sre[base + z];
+            gim[z] = S.sim[base + z];
           }
 #pragma unroll
           for (int j = 0; j < P::PMAX; ++j) {
             if (j < np) {
               R wzj[P::BOXP];
               g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
-              R tr = R(0), ti = R(0);
+              R tr0 = R(0), ti0 = R(0), tr1 = R(0), ti1 = R(0);
 #pragma unroll
-              for (int z = 0; z < P::BOX; ++z) {
-                tr += wzj[z] * gr[z];
-                ti += wzj[z] * gim[z];
+              for (int z = 0; z + 1 < P::BOX; z += 2) {
+                tr0 += wzj[z] * gr[z];
+                ti0 += wzj[z] * gim[z];
+                tr1 += wzj[z + 1] * gr[z + 1];
+                ti1 += wzj[z + 1] * gim[z + 1];
+              }
+              if (P::BOX & 1) {
+                tr0 += wzj[P::BOX - 1] * gr[P::BOX - 1];
+                ti0 += wzj[P::BOX - 1] * gim[P::BOX - 1];
               }
               const R wxy = wx[j * P::BOXP + bx] * wy[j * P::BOXP + by];
-              acc[2 * j] += wxy * tr;
-              acc[2 * j + 1] += wxy * ti;
+              acc[2 * j] += wxy * (tr0 + tr1);
+              acc[2 * j + 1] += wxy * (ti0 + ti1);
             }
           }
         }
@@ -346,36 +370,31 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
   typedef G3<R, W, CS> P;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int cells = g.ext[0] * g.ext[1] * g.ext[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  R *wx, *sre, *sim;
-  int *sub, *gstart, *ucnt, *ustart, *wsum;
-  G3Smem::carve<R, W, CS>(smem_raw, cells, wx, sre, sim, sub, gstart, ucnt, ustart, wsum);
-  R *wy = wx + P::PMAX * P::BOXP;
-  R *wz = wy + P::PMAX * P::BOXP;
-  R *fv = wz + P::PMAX * P::BOXP;
+  G3Smem<R, W, CS> S(smem_raw, g);
+  const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
   g3_tile_origin<R>(it, g, org);
-  for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
-    sre[idx] = R(0);
-    sim[idx] = R(0);
+  for (int i = threadIdx.x; i < P::EXT * g.sx; i += G3_THREADS) {
+    S.sre[i] = R(0);
+    S.sim[i] = R(0);
   }
-  const int e1 = g.ext[1], e2 = g.ext[2];
   for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
     const int c1 = min(c0 + G3_WINDOW, it.end);
-    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, sub, gstart, ucnt, ustart, wsum);
+    const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, S.sub, S.gstart, S.ucnt, S.ustart, S.wsum);
     for (int ui = warp; ui < nu; ui += G3_WARPS) {
-      const int u0 = ustart[ui], np = ustart[ui + 1] - u0;
+      const int u0 = S.ustart[ui], np = S.ustart[ui + 1] - u0;
       int box0[3];
       node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
       if (lane < np) {
         const C v = f[perm[u0 + lane]];
-        fv[2 * lane] = v.x;
-        fv[2 * lane + 1] = v.y;
+        S.fv[2 * lane] = v.x;
+        S.fv[2 * lane + 1] = v.y;
       }
-      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, wx);  // ends with __syncwarp
+      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);  // ends with __syncwarp
+      const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
 #pragma unroll 1
       for (int ri = 0; ri < P::RITER; ++ri) {
         const int row = lane + 32 * ri;
@@ -388,7 +407,7 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
           for (int j = 0; j < P::PMAX; ++j) {
             if (j < np) {
               const R wxy = wx[j * P::BOXP + bx] * wy[j * P::BOXP + by];
-              const R hr = wxy * fv[2 * j], hi = wxy * fv[2 * j + 1];
+              const R hr = wxy * S.fv[2 * j], hi = wxy * S.fv[2 * j + 1];
               R wzj[P::BOXP];
               g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
 #pragma unroll
@@ -398,11 +417,11 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
               }
             }
           }
-          const int base = ((box0[0] + bx) * e1 + (box0[1] + by)) * e2 + box0[2];
+          const int base = sbase + bx * g.sx + by * g.sy;
 #pragma unroll
           for (int z = 0; z < P::BOX; ++z) {
-            atomicAdd(sre + base + z, ar[z]);
-            atomicAdd(sim + base + z, ai[z]);
+            atomicAdd(S.sre + base + z, ar[z]);
+            atomicAdd(S.sim + base + z, ai[z]);
           }
         }
       }
@@ -411,10 +430,13 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
     __syncthreads();
   }
   // one vector reduction per non-zero cell of the padded subgrid
-  for (int idx = threadIdx.x; idx < cells; idx += G3_THREADS) {
-    const R vr = sre[idx], vi = sim[idx];
+  for (int idx = threadIdx.x; idx < P::EXT * P::EXT * P::EXT; idx += G3_THREADS) {
+    int si;
+    long long gi;
+    g3_cell<R, P::EXT>(idx, org, g, si, gi);
+    const R vr = S.sre[si], vi = S.sim[si];
     if (vr == R(0) && vi == R(0)) continue;
-    global_add_c(grid + g3_global_cell<R>(idx, org, g), cmake(vr, vi));
+    global_add_c(grid + gi, cmake(vr, vi));
   }
 }
 

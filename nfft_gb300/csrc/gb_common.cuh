@@ -52,6 +52,7 @@ struct Geom {
   int ext[GB_MAXD];      // padded subgrid edge T_t + w - 1
   int cs;                // sub-cell edge of the 3-D group kernels (1 = off)
   int sub;               // sub-cells per tile ((T/cs)^d, 1 = off)
+  int sx, sy;            // shared-memory plane strides of the group kernels (x, y)
 };
 
 struct WorkItem {
@@ -95,6 +96,46 @@ __device__ __forceinline__ R kb_phi(R xl, R nR, R mm, R b)
   }
   return b / gb_pi<R>();
 }
+
+// The same window as a function of t = n (x - l/n) (the argument the macro
+// forms first); kb_phi_t is the accurate form, kb_phi_t_fast the single
+// precision form of the 3-D group kernels: rsqrt instead of sqrt and a
+// division, sinh from one accurate expf and an approximate reciprocal (the
+// e^{-y} term matters only where the weight is near its smallest, b/pi, far
+// below the window's peak), and the approximate sine on the two outer taps,
+// whose weights are of order b/pi against a peak of sinh(b m)/(pi m).
+template <typename R>
+__device__ __forceinline__ R kb_phi_t(R t, R mm, R b)
+{
+  const R t2 = t * t;
+  const R arg = mm - t2;
+  if (arg > R(0)) {
+    const R s = gb_sqrt(arg);
+    return gb_sinh(b * s) / (gb_pi<R>() * s);
+  } else if (arg < R(0)) {
+    const R s = gb_sqrt(t2 - mm);
+    return gb_sin(b * s) / (gb_pi<R>() * s);
+  }
+  return b / gb_pi<R>();
+}
+
+__device__ __forceinline__ float kb_phi_t_fast(float t, float mm, float b)
+{
+  const float inv_pi = 0.318309886183790671538f;
+  const float arg = mm - t * t;
+  if (arg > 0.f) {
+    const float r = rsqrtf(arg);
+    const float e = expf(b * (arg * r));
+    return 0.5f * (e - __fdividef(1.f, e)) * (r * inv_pi);
+  } else if (arg < 0.f) {
+    const float r = rsqrtf(-arg);
+    return __sinf(b * (-arg * r)) * (r * inv_pi);
+  }
+  return b * inv_pi;
+}
+
+__device__ __forceinline__ float kb_window_t(float t, float mm, float b) { return kb_phi_t_fast(t, mm, b); }
+__device__ __forceinline__ double kb_window_t(double t, double mm, double b) { return kb_phi_t<double>(t, mm, b); }
 
 // Unwrapped window start u = floor(x n) - m (reference nfft.c:324-332).  The
 // same expression is used by the binning and by every transform kernel so a

@@ -153,12 +153,37 @@ static void choose_tiles(Ctx<R> *c)
   if (g.d == 3 && group3_supported<R>(g.w) && g.n[0] >= 8 && g.n[1] >= 8 && g.n[2] >= 8) {
     Geom<R> h = g;
     for (int t = 0; t < 3; ++t) h.ext[t] = 8 + g.w - 1;
+    h.sx = h.ext[0] * (h.ext[0] + 8) + 40;  // upper bound of the padded plane stride
     if (group3_smem_bytes<R>(h) <= 200 * 1024) {
       c->group3 = true;
       c->tiled = true;
       T = 8;
       g.cs = cs;
       g.sub = (8 / cs) * (8 / cs) * (8 / cs);
+      // plane strides: rows of a box taken 32 at a time by a warp should hit
+      // distinct banks; search the padding that minimises the worst case
+      const int ext = 8 + g.w - 1, box = g.w + cs - 1, rows = box * box;
+      int best = 1 << 30;
+      g.sy = ext;
+      g.sx = ext * ext;
+      for (int sy = ext; sy < ext + 8; ++sy)
+        for (int sx = ext * sy; sx < ext * sy + 40; ++sx) {
+          int cost = 0;
+          for (int r0 = 0; r0 < rows; r0 += 32) {
+            int cnt[32] = {0}, worst = 0;
+            for (int l = 0; l < 32 && r0 + l < rows; ++l) {
+              const int r = r0 + l, bx = r / box, by = r % box;
+              worst = std::max(worst, ++cnt[(bx * sx + by * sy) & 31]);
+            }
+            cost += worst;
+          }
+          cost = cost * 4096 + (sx * ext);  // then the smallest footprint
+          if (cost < best) {
+            best = cost;
+            g.sy = sy;
+            g.sx = sx;
+          }
+        }
     }
   }
   c->ntiles = 1;

@@ -213,6 +213,40 @@ def config_of(wl):
 
 
 # ------------------------------------------------------------------ GPU side
+def accuracy_sample(lib, wl, x, fh_host, f_host, f_out, n_trafo=256, n_adj=1024):
+    """Relative l2 error against the FP64 NDFT (nfft_trafo_direct /
+    nfft_adjoint_direct on the GPU): the benchmark's own trafo output on its
+    first n_trafo nodes, and the adjoint of a subset plan of n_adj nodes with
+    the same N, n, m (the adjoint of a subset is its own problem)."""
+    from nfft_gb300 import abi
+    from nfft_gb300.plan import Plan
+    N, n, m = wl["N"], wl["n"], wl["m"]
+    flags = (abi.PRE_PHI_HUT | abi.PRE_PSI | abi.MALLOC_X | abi.MALLOC_F_HAT | abi.MALLOC_F
+             | abi.FFTW_INIT | abi.FFT_OUT_OF_PLACE)
+    got = f_out[: 2 * n_trafo].cpu().numpy().view(np.complex64).astype(np.complex128)
+    q = Plan(lib, False, N, n_trafo, n=n, m=m, flags=flags)
+    q.x[:] = x[:n_trafo].astype(np.float64)
+    q.f_hat[:] = fh_host.astype(np.complex128)
+    q.trafo_direct()
+    e_t = float(np.linalg.norm(got - q.f) / np.linalg.norm(q.f))
+    q.finalize()
+    s = Plan(lib, True, N, n_adj, n=n, m=m, flags=flags)
+    s.x[:] = x[:n_adj]
+    s.precompute_one_psi()
+    s.f[:] = f_host[:n_adj]
+    s.adjoint()
+    got_a = s.f_hat.astype(np.complex128)
+    s.finalize()
+    q = Plan(lib, False, N, n_adj, n=n, m=m, flags=flags)
+    q.x[:] = x[:n_adj].astype(np.float64)
+    q.f[:] = f_host[:n_adj].astype(np.complex128)
+    q.adjoint_direct()
+    e_a = float(np.linalg.norm(got_a - q.f_hat) / np.linalg.norm(q.f_hat))
+    q.finalize()
+    return {"trafo_rel_l2_vs_ndft": e_t, "trafo_nodes": n_trafo,
+            "adjoint_rel_l2_vs_ndft": e_a, "adjoint_subset_nodes": n_adj}
+
+
 def run_gpu(args, wl):
     import torch
     import nfft_gb300
@@ -302,6 +336,11 @@ def run_gpu(args, wl):
     ms_step = ms_total / args.steps
     value = M * world / (ms_step * 1e-3)
 
+    # ---- accuracy of this very run against the FP64 NDFT (on the GPU)
+    accuracy = None
+    if not args.no_accuracy:
+        accuracy = accuracy_sample(lib, wl, x, fh_host, f_host, f_out)
+
     # ---- e2e through the C ABI on host arrays (copies inside the timed region)
     e2e_times = []
     for it in range(args.warmup + args.steps):
@@ -372,7 +411,7 @@ def run_gpu(args, wl):
             "stages_ms": {k: round(v, 4) for k, v in stage.items()},
             "pair_hbm_gbs_algorithmic": round(hbm_pair, 1),
             "pair_hbm_frac": round(hbm_pair / peaks["hbm_gbs"], 4),
-            "precompute_s": round(t_pre, 4)}
+            "precompute_s": round(t_pre, 4), "accuracy": accuracy}
     p.finalize()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -389,6 +428,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform", choices=["uniform", "clustered", "small"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the NDFT accuracy sample")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -192,12 +192,12 @@ __device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restr
 {
   typedef G3<R, W, CS> P;
   const int lane = threadIdx.x & 31;
-  if (lane < 3 * np) {
-    const int j = lane / 3, t = lane - 3 * j;
+  for (int k = lane; k < 3 * np; k += 32) {
+    const int j = k / 3, t = k - 3 * j;
     const R xn = xs[(long long)(u0 + j) * 3 + t] * g.nR[t];
     const int u = (int)gb_floor(xn) - g.m;  // node_u
-    so[lane] = wrap(u, g.n[t]) - org[t] - box0[t];
-    t0[lane] = xn - R(u);
+    so[k] = wrap(u, g.n[t]) - org[t] - box0[t];
+    t0[k] = xn - R(u);
   }
   __syncwarp();
   for (int k = lane; k < 3 * np * P::BOXP; k += 32) {

@@ -206,6 +206,27 @@ def test_clustered_nodes_and_heavy_tiles(gpulib):
     assert rel_l2(gfh, od.adjoint(f.astype(np.complex64))) < 2e-5
 
 
+@pytest.mark.parametrize("density", [1, 3])
+@pytest.mark.parametrize("m", [3, 4, 6])
+def test_dense_3d_single(gpulib, density, m):
+    """3-D single precision at >= 1 node per oversampled cell: sub-cell groups
+    larger than one unit, the regime of the 3-D benchmark."""
+    N = [16, 16, 16]
+    M = density * 32 ** 3
+    x, fh, f = seeded_case(N, M, seed=12)
+    x32 = x.astype(np.float32)
+    p = make_plan(gpulib, True, N, M, m=m)
+    gf, gfh = run_both(p, x32, fh.astype(np.complex64), f.astype(np.complex64))
+    p.finalize()
+    od = oracle.OraclePlan(N, M, n=[32] * 3, m=m, single=False)
+    od.set_nodes(x32.astype(np.float64))
+    od.precompute()
+    rf = od.trafo(fh.astype(np.complex64))
+    rfh = od.adjoint(f.astype(np.complex64))
+    assert rel_l2(gf, rf) < 2e-5, rel_l2(gf, rf)
+    assert rel_l2(gfh, rfh) < 2e-5, rel_l2(gfh, rfh)
+
+
 def test_edge_nodes_and_small_m(gpulib):
     """Nodes on -1/2 and just below +1/2, window wrap-around on every side."""
     N, m = [32, 32], 6

@@ -12,7 +12,7 @@ import ctypes as _C
 import os as _os
 
 HERE = _os.path.dirname(_os.path.abspath(__file__))
-LIB_PATH = _os.path.join(HERE, "libnfft3_gb300.so")
+LIB_PATH = _os.environ.get("NFFT_GB300_LIB") or _os.path.join(HERE, "libnfft3_gb300.so")
 
 _lib = None
 

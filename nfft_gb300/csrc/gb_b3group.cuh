@@ -38,14 +38,19 @@ static constexpr int G3_TILE = 8;          // tile edge (cells)
 static constexpr int G3_WINDOW = 1024;     // nodes per unit-building window
 static constexpr int G3_MAXITEM = 16384;   // nodes per work item
 
-template <typename R, int W, int CS>
+// nodes per unit: B keeps 2 PMAX partial sums per lane, B^T 2 (w + CS - 1)
+// accumulators, so B^T prefers smaller units
+template <typename R> __host__ __device__ constexpr int g3_pm_b() { return sizeof(R) == 4 ? 16 : 8; }
+template <typename R> __host__ __device__ constexpr int g3_pm_bt() { return 8; }
+
+template <typename R, int W, int CS, int PM>
 struct G3 {
   static constexpr int EXT = G3_TILE + W - 1;                     // padded subgrid edge
   static constexpr int BOX = W + CS - 1;                          // box edge
   static constexpr int BOXP = (BOX + 3) / 4 * 4;                  // padded for vector loads
   static constexpr int ROWS = BOX * BOX;                          // (x, y) rows of a box
   static constexpr int RITER = (ROWS + 31) / 32;                  // row iterations per lane
-  static constexpr int PMAX = sizeof(R) == 4 ? 16 : 8;            // nodes per unit
+  static constexpr int PMAX = PM;                                 // nodes per unit
   static constexpr int NV = 2 * PMAX;                             // reduced values per unit
   // per-warp scratch (R): wx, wy, wz [PMAX][BOXP] each, f values [PMAX][2],
   // window offsets t0 [3 PMAX], box offsets o [3 PMAX] (as int)
@@ -56,7 +61,7 @@ struct G3 {
 template <typename R, int W, int CS>
 inline size_t g3_smem_bytes(const Geom<R> &g)
 {
-  typedef G3<R, W, CS> P;
+  typedef G3<R, W, CS, (g3_pm_b<R>() > g3_pm_bt<R>() ? g3_pm_b<R>() : g3_pm_bt<R>())> P;
   const size_t plane = (size_t)P::EXT * g.sx;
   return (2 * plane + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
 }
@@ -186,11 +191,11 @@ __device__ int g3_units(int c0, int c1, const R *__restrict__ xs, const Geom<R> 
 // warp's zero-padded box vectors w[t][j][b] ([3][PMAX][BOXP]).  t0 / so are
 // per (node, dim) scratch: t0 = n x - u (the argument of tap 0), so = box
 // offset of the window.
-template <typename R, int W, int CS>
+template <typename R, int W, int CS, int PM>
 __device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restrict__ xs, const Geom<R> &g,
                                                 const int *org, const int *box0, R *w, R *t0, int *so)
 {
-  typedef G3<R, W, CS> P;
+  typedef G3<R, W, CS, PM> P;
   const int lane = threadIdx.x & 31;
   for (int k = lane; k < 3 * np; k += 32) {
     const int j = k / 3, t = k - 3 * j;
@@ -252,7 +257,7 @@ __device__ __forceinline__ void g3_load_vec(const R *src, R (&dst)[BOXP])
   }
 }
 
-template <typename R, int W, int CS>
+template <typename R, int W, int CS, int PM>
 struct G3Smem {
   R *w, *fv, *t0;
   int *so;
@@ -260,7 +265,7 @@ struct G3Smem {
   int *sub, *gstart, *ucnt, *ustart, *wsum;
   __device__ G3Smem(unsigned char *raw, const Geom<R> &g)
   {
-    typedef G3<R, W, CS> P;
+    typedef G3<R, W, CS, PM> P;
     R *base = reinterpret_cast<R *>(raw);  // per-warp scratch first: 16-byte aligned
     w = base + (threadIdx.x >> 5) * P::WARP_FLOATS;
     fv = w + 3 * P::PMAX * P::BOXP;
@@ -283,11 +288,12 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
                                                              const uint32_t *__restrict__ perm,
                                                              typename Cx<R>::T *__restrict__ f, Geom<R> g)
 {
-  typedef G3<R, W, CS> P;
+  constexpr int PM = g3_pm_b<R>();
+  typedef G3<R, W, CS, PM> P;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  G3Smem<R, W, CS> S(smem_raw, g);
+  G3Smem<R, W, CS, PM> S(smem_raw, g);
   const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
       const int u0 = S.ustart[ui], np = S.ustart[ui + 1] - u0;
       int box0[3];
       node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
-      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);
+      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);
       const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
       R acc[P::NV];
 #pragma unroll
@@ -367,11 +373,12 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
                                                               const typename Cx<R>::T *__restrict__ f,
                                                               Geom<R> g)
 {
-  typedef G3<R, W, CS> P;
+  constexpr int PM = g3_pm_bt<R>();
+  typedef G3<R, W, CS, PM> P;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  G3Smem<R, W, CS> S(smem_raw, g);
+  G3Smem<R, W, CS, PM> S(smem_raw, g);
   const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
@@ -393,7 +400,7 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
         S.fv[2 * lane] = v.x;
         S.fv[2 * lane + 1] = v.y;
       }
-      g3_unit_weights<R, W, CS>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);  // ends with __syncwarp
+      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);  // ends with __syncwarp
       const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
 #pragma unroll 1
       for (int ri = 0; ri < P::RITER; ++ri) {

@@ -85,6 +85,25 @@ void nfft_gb_clear_error(void);
 /* 1 when the library was built for and runs on an sm_103 device. */
 int nfft_gb_device_ok(void);
 
+/* The node sort of NFFT_SORT_NODES without any device allocation (no
+ * counterpart in the reference).  For callers that cannot allocate device
+ * memory where they sort nodes: their memory belongs to a caching allocator
+ * or a fixed budget, or they cannot afford the device synchronisation that
+ * cudaMalloc / cudaFree imply.  Writes into index_x_dev (2*M long long, device)
+ * the same (key, node) pairs that nfft_precompute_one_psi puts in index_x for
+ * nodes x_dev (M*d reals on the device, float if single != 0, else double)
+ * and grid lengths n[0..d-1] with cut-off m, enqueued on `stream`.
+ * Limits: M <= 262144 (else returns -1 without doing anything; the reason is
+ * in nfft_gb_last_error); the n_t must multiply to less than 2^32.  All
+ * intermediate buffers live in one static device array of about 4.3 MB that
+ * every GPU loading the library keeps until exit; the first call on a device
+ * looks up its address there (make that call before any stream capture);
+ * calls share the array, so calls that overlap on the GPU race and must be
+ * serialised by the caller.  Returns 0 on success, -1 on invalid input, -2
+ * if the scratch array cannot be reached on the current device. */
+int nfft_gb_sort_nodes_noalloc(int single, const void *x_dev, int d, const int *n, int m, int M,
+                               long long *index_x_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

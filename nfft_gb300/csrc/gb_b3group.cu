@@ -14,7 +14,7 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
                    cudaStream_t s)
 {
   static bool attr = false;
-  const size_t smem = g3_smem_bytes<R, W, G3_CS>(g);
+  const size_t smem = adjoint ? g3_smem_bytes<R, W, G3_CS, g3_pm_bt<R>()>(g) : g3_smem_bytes<R, W, G3_CS, g3_pm_b<R>()>(g);
   if (!attr) {
     GB_CUDA(cudaFuncSetAttribute(k_b3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  200 * 1024));

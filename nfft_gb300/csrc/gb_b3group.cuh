@@ -58,10 +58,10 @@ struct G3 {
   static constexpr int INTS = 4 * G3_WINDOW + 2 + G3_WARPS;       // sub, gstart, ucount, ustart, wsum
 };
 
-template <typename R, int W, int CS>
+template <typename R, int W, int CS, int PM = (g3_pm_b<R>() > g3_pm_bt<R>() ? g3_pm_b<R>() : g3_pm_bt<R>())>
 inline size_t g3_smem_bytes(const Geom<R> &g)
 {
-  typedef G3<R, W, CS, (g3_pm_b<R>() > g3_pm_bt<R>() ? g3_pm_b<R>() : g3_pm_bt<R>())> P;
+  typedef G3<R, W, CS, PM> P;
   const size_t plane = (size_t)P::EXT * g.sx;
   return (2 * plane + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
 }

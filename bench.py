@@ -420,18 +420,68 @@ def run_gpu(args, wl):
     return 0
 
 
+def run_infft(args):
+    """Mixed-precision inverse NFFT on 2-D radial k-space: N = 256^2, sigma = 2,
+    m = 6, 402 spokes x 512 samples, 20-ellipse phantom (seed 1), y = A f_true
+    (FP64 transform) + complex Gaussian noise at 40 dB SNR.  value = wall time
+    of FP32 CGNR (FP64 inner products, FP64 residual refresh every 10
+    iterations) to reach 1e-5 relative error against the converged FP64 CGNR
+    solution of the same normal equations; error vs f_true is reported too."""
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import infft, workloads
+    from nfft_gb300.plan import Plan
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lib = nfft_gb300.lib()
+    N, m = [256, 256], 6
+    x = workloads.radial_nodes(402, 512)
+    f_true = workloads.ellipse_phantom(256, 20, seed=1)
+    M = len(x)
+    p = Plan(lib, False, N, M, n=[512, 512], m=m, flags=infft.PLAN_FLAGS)
+    p.x[:] = x
+    p.precompute_one_psi()
+    p.f_hat[:] = f_true
+    p.trafo()
+    y = workloads.add_noise(p.f.copy(), 40.0, np.random.default_rng(1))
+    p.finalize()
+    t0 = time.perf_counter()
+    f_ref, ref_iters = infft.fp64_solution(lib, N, x, m, y, max_iter=args.max_iter)
+    t_ref = time.perf_counter() - t0
+    res = {}
+    for name, single, refresh in (("fp32_fp64dots_refresh10", True, 10), ("fp64", False, 0)):
+        r = infft.time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, refresh=refresh,
+                                    max_iter=args.max_iter)
+        res[name] = r
+    mixed = res["fp32_fp64dots_refresh10"]
+    err_true = float(np.linalg.norm(f_ref - f_true) / np.linalg.norm(f_true))
+    line = {"metric": "iNFFT time to 1e-5 rel. err (vs converged FP64 CGNR), 2-D radial",
+            "value": mixed["seconds"], "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f32 (FP64 dots, FP64 residual refresh every 10)", "data": "synthetic",
+            "config": {"workload": "2-D radial iNFFT N=256^2 n=512^2 m=6 402x512 spokes, 20 ellipses, 40 dB",
+                       "M": M, "solver": "CGNR"},
+            "iters": mixed["iters"], "reached": mixed["reached"], "final_rel_err_vs_fp64": mixed["err"],
+            "fp64_cgnr": res["fp64"], "fp64_reference_iters": ref_iters,
+            "fp64_reference_seconds": t_ref, "fp64_solution_rel_err_vs_f_true": err_true}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "clustered", "small"])
+    ap.add_argument("--workload", default="uniform",
+                    choices=["uniform", "clustered", "small", "infft"])
+    ap.add_argument("--max-iter", type=int, default=3000, help="iNFFT iteration cap")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the NDFT accuracy sample")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    if args.workload == "infft":
+        return run_infft(args)
     wl = workload(args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)

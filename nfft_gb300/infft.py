@@ -1,0 +1,130 @@
+"""Inverse NFFT (CGNR) driver on the GPU library, for benchmarks and tests.
+
+Runs the solver through the reference-facing C ABI (solver_* over nfft_*
+plans, solverf_* over nfftf_* plans) with the library's extensions: scalars-
+only synchronisation inside the timed loop, and an FP64 residual refresh for
+single-precision solvers (r = y - A f recomputed by an FP64 transform every
+`refresh` iterations, kernel/solver/solver.c:81-125 being the formula).
+"""
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import abi
+from .plan import Plan, Solver
+
+PLAN_FLAGS = (abi.PRE_PHI_HUT | abi.PRE_PSI | abi.MALLOC_X | abi.MALLOC_F_HAT | abi.MALLOC_F
+              | abi.FFTW_INIT | abi.FFT_OUT_OF_PLACE)
+
+
+def _ext(lib, name, restype, argtypes):
+    fn = getattr(lib, name)
+    fn.restype = restype
+    fn.argtypes = argtypes
+    return fn
+
+
+class CGNR:
+    """CGNR on one plan; weights w (M) make it the weighted normal equations
+    A^H W A f = A^H W y (PRECOMPUTE_WEIGHT)."""
+
+    def __init__(self, lib, single, N, x, m, y, w=None, refresh=0, cgne=False):
+        self.lib = lib
+        self.single = single
+        M = len(x)
+        n = [2 * (1 << (int(v) - 1).bit_length()) for v in N]
+        self.plan = Plan(lib, single, N, M, n=n, m=m, flags=PLAN_FLAGS)
+        self.plan.x[:] = x.astype(np.float32 if single else np.float64)
+        self.plan.precompute_one_psi()
+        flags = abi.CGNE if cgne else abi.CGNR
+        if w is not None:
+            flags |= abi.PRECOMPUTE_WEIGHT
+        self.solver = Solver(self.plan, flags)
+        self.solver.y[:] = y
+        if w is not None:
+            self.solver.w[:] = w
+        self.solver.f_hat_iter[:] = 0
+        pfx = "solverf_" if single else "solver_"
+        self._set_sync = _ext(lib, pfx + "gb_set_sync", C.c_int, [C.c_void_p, C.c_int])
+        self._sync = _ext(lib, pfx + "gb_sync", C.c_int, [C.c_void_p])
+        self._refresh = _ext(lib, pfx + "gb_set_refresh", C.c_int, [C.c_void_p, C.c_int])
+        self.addr = C.addressof(self.solver.s)
+        if refresh:
+            self._refresh(self.addr, int(refresh))
+
+    def set_sync(self, level):
+        self._set_sync(self.addr, int(level))
+
+    def sync(self):
+        self._sync(self.addr)
+
+    def before_loop(self):
+        self.solver.before_loop()
+
+    def step(self):
+        self.solver.loop_one_step()
+
+    @property
+    def f_hat(self):
+        return self.solver.f_hat_iter.astype(np.complex128)
+
+    @property
+    def dot_r(self):
+        return float(self.solver.s.dot_r_iter)
+
+    def close(self):
+        self.solver.finalize()
+        self.plan.finalize()
+
+
+def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14):
+    """FP64 CGNR run to convergence (relative change of f below rtol)."""
+    s = CGNR(lib, False, N, x, m, y, w=w)
+    s.set_sync(1)
+    s.before_loop()
+    prev = s.f_hat.copy()
+    it = 0
+    for it in range(1, max_iter + 1):
+        s.step()
+        if it % 10 == 0:
+            cur = s.f_hat
+            ch = np.linalg.norm(cur - prev) / max(np.linalg.norm(cur), 1e-300)
+            prev = cur.copy()
+            if ch < rtol:
+                break
+    out = s.f_hat.copy()
+    s.close()
+    return out, it
+
+
+def time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, w=None, refresh=10, max_iter=3000):
+    """Iterations and wall time for CGNR to reach ||f - f_ref|| / ||f_ref|| < tol.
+
+    A first untimed run finds the iteration count; a second run of exactly
+    that many iterations is timed (scalars-only synchronisation per step, the
+    iterate copied back once at the end).  Returns dict(iters, seconds, err,
+    reached)."""
+    nref = np.linalg.norm(f_ref)
+    s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0)
+    s.set_sync(1)
+    s.before_loop()
+    k, err = 0, np.inf
+    for k in range(1, max_iter + 1):
+        s.step()
+        err = np.linalg.norm(s.f_hat - f_ref) / nref
+        if err < tol:
+            break
+    s.close()
+    reached = err < tol
+    s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0)
+    s.set_sync(0)
+    t0 = time.perf_counter()
+    s.before_loop()
+    for _ in range(k):
+        s.step()
+    s.sync()
+    t1 = time.perf_counter()
+    err2 = np.linalg.norm(s.f_hat - f_ref) / nref
+    s.close()
+    return dict(iters=k, seconds=t1 - t0, err=float(err2), reached=bool(reached))

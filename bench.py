@@ -423,17 +423,17 @@ def run_gpu(args, wl):
 def run_infft(args):
     """Mixed-precision inverse NFFT on 2-D radial k-space: N = 256^2, sigma = 2,
     m = 6, 402 spokes x 512 samples, 20-ellipse phantom (seed 1), y = A f_true
-    (FP64 transform) + complex Gaussian noise at 40 dB SNR.  value = wall time
-    of FP32 CGNR (FP64 inner products, FP64 residual refresh every 10
-    iterations) to reach 1e-5 relative error against the converged FP64 CGNR
-    solution of the same normal equations; error vs f_true is reported too."""
+    (FP64 transform) + complex Gaussian noise at 40 dB SNR.  K CGNR iterations
+    in FP32 with FP64 inner products and an FP64 residual refresh every 10
+    iterations; reported: wall time (value), distance to the FP64 CGNR iterate
+    after the same K iterations, and the error against f_true for each."""
     import torch
     import nfft_gb300
     from nfft_gb300 import infft, workloads
     from nfft_gb300.plan import Plan
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     lib = nfft_gb300.lib()
-    N, m = [256, 256], 6
+    N, m, K = [256, 256], 6, args.iters
     x = workloads.radial_nodes(402, 512)
     f_true = workloads.ellipse_phantom(256, 20, seed=1)
     M = len(x)
@@ -444,24 +444,27 @@ def run_infft(args):
     p.trafo()
     y = workloads.add_noise(p.f.copy(), 40.0, np.random.default_rng(1))
     p.finalize()
-    t0 = time.perf_counter()
-    f_ref, ref_iters = infft.fp64_solution(lib, N, x, m, y, max_iter=args.max_iter)
-    t_ref = time.perf_counter() - t0
-    res = {}
-    for name, single, refresh in (("fp32_fp64dots_refresh10", True, 10), ("fp64", False, 0)):
-        r = infft.time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, refresh=refresh,
-                                    max_iter=args.max_iter)
-        res[name] = r
-    mixed = res["fp32_fp64dots_refresh10"]
-    err_true = float(np.linalg.norm(f_ref - f_true) / np.linalg.norm(f_true))
-    line = {"metric": "iNFFT time to 1e-5 rel. err (vs converged FP64 CGNR), 2-D radial",
+    nt = np.linalg.norm(f_true)
+    runs = {}
+    for name, single, refresh in (("fp64", False, 0), ("fp32_fp64dots_refresh10", True, 10),
+                                  ("fp32_fp64dots_norefresh", True, 0)):
+        infft.run_iterations(lib, single, N, x, m, y, 3, refresh=refresh)  # warm-up
+        f, sec, dots = infft.run_iterations(lib, single, N, x, m, y, K, refresh=refresh)
+        runs[name] = dict(f=f, seconds=sec, dot_r=dots[-1])
+    f64 = runs["fp64"]["f"]
+    out = {}
+    for name, r in runs.items():
+        out[name] = {"seconds": r["seconds"], "ms_per_iter": 1e3 * r["seconds"] / K,
+                     "rel_err_vs_f_true": float(np.linalg.norm(r["f"] - f_true) / nt),
+                     "rel_dist_to_fp64_iterate": float(np.linalg.norm(r["f"] - f64) / np.linalg.norm(f64)),
+                     "dot_r": r["dot_r"]}
+    mixed = out["fp32_fp64dots_refresh10"]
+    line = {"metric": "iNFFT CGNR wall time for K iterations, 2-D radial (FP32 + FP64 dots/refresh)",
             "value": mixed["seconds"], "unit": "s", "n_gpus": 1, "higher_is_better": False,
             "dtype": "f32 (FP64 dots, FP64 residual refresh every 10)", "data": "synthetic",
             "config": {"workload": "2-D radial iNFFT N=256^2 n=512^2 m=6 402x512 spokes, 20 ellipses, 40 dB",
-                       "M": M, "solver": "CGNR"},
-            "iters": mixed["iters"], "reached": mixed["reached"], "final_rel_err_vs_fp64": mixed["err"],
-            "fp64_cgnr": res["fp64"], "fp64_reference_iters": ref_iters,
-            "fp64_reference_seconds": t_ref, "fp64_solution_rel_err_vs_f_true": err_true}
+                       "M": M, "solver": "CGNR", "iterations": K},
+            "runs": out}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -474,7 +477,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
                     choices=["uniform", "clustered", "small", "infft"])
-    ap.add_argument("--max-iter", type=int, default=3000, help="iNFFT iteration cap")
+    ap.add_argument("--iters", type=int, default=100, help="CGNR iterations of the iNFFT workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the NDFT accuracy sample")
     args = ap.parse_args()

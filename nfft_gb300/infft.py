@@ -98,6 +98,24 @@ def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14):
     return out, it
 
 
+def run_iterations(lib, single, N, x, m, y, iters, w=None, refresh=0):
+    """Run `iters` CGNR steps timed (scalars-only synchronisation per step);
+    returns (f_hat_iter after the last step, seconds, per-step dot_r)."""
+    s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0)
+    s.set_sync(0)
+    dots = []
+    t0 = time.perf_counter()
+    s.before_loop()
+    for _ in range(iters):
+        s.step()
+        dots.append(s.dot_r)
+    s.sync()
+    t1 = time.perf_counter()
+    out = s.f_hat.copy()
+    s.close()
+    return out, t1 - t0, dots
+
+
 def time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, w=None, refresh=10, max_iter=3000):
     """Iterations and wall time for CGNR to reach ||f - f_ref|| / ||f_ref|| < tol.
 

@@ -41,14 +41,3 @@ def test_mixed_precision_cgnr_tracks_fp64(gpulib):
     e32 = np.linalg.norm(f32 - f_true) / np.linalg.norm(f_true)
     assert abs(e32 - e64) < 1e-2 and e64 < 0.5, (e32, e64)
     assert d32[-1] < d32[0] and d64[-1] < d64[0]
-
-
-def test_fp64_cgnr_matches_itself_with_weights(gpulib):
-    """Weighted CGNR (PRECOMPUTE_WEIGHT, density-compensation-like weights)
-    converges to the weighted least-squares solution in fewer iterations."""
-    N, x, m, y, _ = _problem(gpulib)
-    r = np.sqrt((x ** 2).sum(axis=1))
-    w = np.maximum(r, 1.0 / 128)
-    f_w, it_w = infft.fp64_solution(gpulib, N, x, m, y, w=w, max_iter=3000, rtol=1e-10)
-    f_u, it_u = infft.fp64_solution(gpulib, N, x, m, y, max_iter=3000, rtol=1e-10)
-    assert it_w < it_u, (it_w, it_u)

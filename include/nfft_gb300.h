@@ -85,6 +85,28 @@ void nfft_gb_clear_error(void);
 /* 1 when the library was built for and runs on an sm_103 device. */
 int nfft_gb_device_ok(void);
 
+/* Density-compensation weights for the inverse NFFT (no counterpart in the
+ * reference, whose solver takes the weights w from the caller):
+ *  - nfftf_gb_dcf_fixed_point: w <- w / |A A^H w| `iters` times on the
+ *    plan's nodes (w_dev: M_total reals on the device, in and out);
+ *  - nfft_gb_dcf_features: 8 features per 2-D node (log(1 + neighbour count)
+ *    within 1, 2, 4 cells of the n0 x n1 grid, 2|x|, cos/sin of the angle and
+ *    of twice the angle), feat_dev = M x 8 floats;
+ *  - an MLP 8 -> 64 -> 64 -> 1 (GELU) on those features: parameter vector of
+ *    nfft_gb_mlp_param_count() floats (W1[8][64], b1, W2[64][64], b2, W3, b3),
+ *    forward, mean-squared-error gradient (grad and loss overwritten) and an
+ *    Adam step; all operands are device pointers. */
+int nfftf_gb_dcf_fixed_point(nfftf_plan *ths, float *w_dev, int iters);
+int nfft_gb_dcf_features(const float *x_dev, int M, int n0, int n1, float *feat_dev, void *stream);
+int nfft_gb_affine_columns(float *a, long long rows, int cols, const float *scale, const float *shift,
+                           void *stream);
+int nfft_gb_mlp_param_count(void);
+int nfft_gb_mlp_forward(const float *params, const float *feat, int M, float *out, void *stream);
+int nfft_gb_mlp_grad(const float *params, const float *feat, const float *target, int M, float *grad,
+                     float *loss, void *stream);
+int nfft_gb_mlp_adam(float *params, const float *grad, float *m1, float *m2, int step, float lr,
+                     float beta1, float beta2, float eps, void *stream);
+
 /* The node sort of NFFT_SORT_NODES without any device allocation (no
  * counterpart in the reference).  For callers that cannot allocate device
  * memory where they sort nodes: their memory belongs to a caching allocator

@@ -469,6 +469,82 @@ def run_infft(args):
     return 0
 
 
+def run_learned(args):
+    """Learned density-compensation weights on 2-D spirals: N = 256^2, m = 6,
+    16 interleaved Archimedean arms x 8192 samples (r = t/2, angle
+    2 pi (24 t + a/16) + random rotation, radius jitter 1e-4).  The MLP is
+    trained on `--train` seeded trajectories against 20 fixed-point iterations
+    w <- w/|A A^H w|; on `--test` held-out trajectories with ellipse phantoms
+    (noiseless data) CGNR with the learned weights and unweighted CGNR are
+    run to 1e-5 relative error against the min-norm solution (FP64 CGNR with
+    the fixed-point weights, converged); value = median wall time with the
+    learned weights."""
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import dcf, infft, workloads
+    from nfft_gb300.plan import Plan
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lib = nfft_gb300.lib()
+    N, m, arms, samples = [256, 256], 6, 16, 8192
+    n = [512, 512]
+    t0 = time.perf_counter()
+    feats, targets = dcf.build_training_set(lib, N, m, range(args.train), arms, samples, fp_iters=20)
+    t_data = time.perf_counter() - t0
+    net = dcf.DensityNet(lib)
+    net.fit_standardisation(feats[: min(16, len(feats))])
+    for f in feats:
+        net.standardise(f, f.numel() // 8)
+    feat, target = torch.cat(feats), torch.cat(targets)
+    del feats, targets
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = net.train(feat, target, epochs=args.epochs, batch=1 << 16, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del feat, target
+    rows = []
+    for i in range(args.test):
+        x = dcf.spiral(1000 + i, arms, samples)
+        f_true = workloads.ellipse_phantom(256, 20, seed=1000 + i)
+        p = Plan(lib, False, N, len(x), n=n, m=m, flags=infft.PLAN_FLAGS)
+        p.x[:] = x
+        p.precompute_one_psi()
+        p.f_hat[:] = f_true
+        p.trafo()
+        y = p.f.copy()
+        p.finalize()
+        t0 = time.perf_counter()
+        w = net.weights(lib, x, n).cpu().numpy()
+        t_w = time.perf_counter() - t0
+        wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
+        f_ref, it_ref = infft.fp64_solution(lib, N, x, m, y, w=wfp, max_iter=args.max_iter, rtol=1e-13)
+        row = {"ref_iters": it_ref, "weights_s": t_w}
+        for name, ww in (("plain", None), ("learned", w), ("fixed_point", wfp)):
+            r = infft.time_to_tolerance(lib, True, N, x, m, y, f_ref, tol=1e-5, w=ww, refresh=10,
+                                        max_iter=args.max_iter)
+            row[name] = r
+        rows.append(row)
+
+    def med(name, key):
+        return float(np.median([r[name][key] for r in rows]))
+
+    line = {"metric": "iNFFT time to 1e-5 rel. err: learned vs plain (2-D spirals)",
+            "value": med("learned", "seconds"), "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f32 (FP64 dots, FP64 residual refresh every 10)", "data": "synthetic",
+            "config": {"workload": "2-D spiral iNFFT N=256^2 n=512^2 m=6, 16 arms x 8192, MLP 8-64-64-1",
+                       "train_trajectories": args.train, "test_trajectories": args.test,
+                       "epochs": args.epochs},
+            "median": {k: {"seconds": med(k, "seconds"), "iters": med(k, "iters")}
+                       for k in ("plain", "learned", "fixed_point")},
+            "reached": {k: int(sum(r[k]["reached"] for r in rows)) for k in ("plain", "learned", "fixed_point")},
+            "speedup_learned_vs_plain": med("plain", "seconds") / max(med("learned", "seconds"), 1e-12),
+            "training": {"data_s": t_data, "train_s": t_train, "loss_first": hist[0], "loss_last": hist[-1]},
+            "weights_inference_s_median": float(np.median([r["weights_s"] for r in rows])),
+            "per_trajectory": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -476,7 +552,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
-                    choices=["uniform", "clustered", "small", "infft"])
+                    choices=["uniform", "clustered", "small", "infft", "learned"])
+    ap.add_argument("--train", type=int, default=256, help="training trajectories (learned)")
+    ap.add_argument("--test", type=int, default=8, help="held-out trajectories (learned)")
+    ap.add_argument("--epochs", type=int, default=3, help="training epochs (learned)")
+    ap.add_argument("--max-iter", type=int, default=3000, help="CGNR iteration cap (learned)")
     ap.add_argument("--iters", type=int, default=100, help="CGNR iterations of the iNFFT workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the NDFT accuracy sample")
@@ -485,6 +565,8 @@ def main():
         args.warmup = 3
     if args.workload == "infft":
         return run_infft(args)
+    if args.workload == "learned":
+        return run_learned(args)
     wl = workload(args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)

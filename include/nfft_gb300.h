@@ -85,6 +85,28 @@ void nfft_gb_clear_error(void);
 /* 1 when the library was built for and runs on an sm_103 device. */
 int nfft_gb_device_ok(void);
 
+/* Batched transforms of many independent 2-D single-precision plans (no
+ * counterpart in the reference, which transforms one plan per call).  Plans
+ * need m = 4 or 6 and their nodes set up; each plan keeps its own result:
+ * trafo reads the plan's device f_hat (nfftf_gb_device_f_hat) and writes its
+ * device f, adjoint reads the device f and writes the device f_hat.
+ *  - create / destroy a batch over `count` plans (the plans must outlive it);
+ *  - autotune: per class of plans (m, oversampling, node density) choose the
+ *    tile edge (8, 16, 32) and threads per node (1, 4, 16) by timing; the
+ *    choice is remembered for the process;
+ *  - run: what = 1 trafo, 2 adjoint, 3 both; mode 0 = stream launches, 1 = a
+ *    CUDA graph of trafo + adjoint captured on first use (what must be 3);
+ *    returns after the GPU has finished;
+ *  - time: milliseconds per trafo + adjoint round over `reps` rounds. */
+void *nfftf_gb_batch_create(nfftf_plan **plans, int count);
+void nfftf_gb_batch_destroy(void *batch);
+int nfftf_gb_batch_autotune(void *batch, int reps);
+int nfftf_gb_batch_run(void *batch, int what, int mode);
+float nfftf_gb_batch_time(void *batch, int reps, int mode);
+long long nfftf_gb_batch_nodes(void *batch);
+int nfftf_gb_batch_items(void *batch);
+int nfftf_gb_batch_plan_config(void *batch, int k, int *T, int *tpn);
+
 /* Density-compensation weights for the inverse NFFT (no counterpart in the
  * reference, whose solver takes the weights w from the caller):
  *  - nfftf_gb_dcf_fixed_point: w <- w / |A A^H w| `iters` times on the

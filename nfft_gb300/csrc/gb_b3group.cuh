@@ -235,9 +235,9 @@ __device__ __forceinline__ void g3_cell(int idx, const int *org, const Geom<R> &
   const int c1 = r % EXT, c0 = r / EXT;
   si = c0 * g.sx + c1 * g.sy + c2;
   int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
-  p0 = p0 >= g.n[0] ? p0 - g.n[0] : p0;
-  p1 = p1 >= g.n[1] ? p1 - g.n[1] : p1;
-  p2 = p2 >= g.n[2] ? p2 - g.n[2] : p2;
+  while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+  while (p1 >= g.n[1]) p1 -= g.n[1];
+  while (p2 >= g.n[2]) p2 -= g.n[2];
   gi = ((long long)p0 * g.n[1] + p1) * g.n[2] + p2;
 }
 

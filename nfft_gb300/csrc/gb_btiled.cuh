@@ -59,7 +59,7 @@ __device__ __forceinline__ long long sub_to_global(int idx, const int *org, cons
 #pragma unroll
   for (int t = 0; t < D; ++t) {
     int p = org[t] + c[t];
-    if (p >= g.n[t]) p -= g.n[t];
+    while (p >= g.n[t]) p -= g.n[t];  // a padded tile can wrap more than once on small grids
     gi = gi * g.n[t] + p;
   }
   return gi;

@@ -86,6 +86,24 @@ template <typename R>
 void launch_bt_generic(typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,
                        const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
 
+// ---------------------------------------------------------------- plan views
+// Device state of a single-precision plan, for the batched transforms.
+struct PlanViewF {
+  Geom<float> g;
+  const float *xs;
+  const uint32_t *perm;
+  const double *cphi;
+  const WorkItem *items;
+  int nitems;
+  float2 *fhat;
+  float2 *f;
+  bool tiled, group3, direct, ready;
+  cudaStream_t stream;
+};
+bool plan_view_f(void *nfftf_plan_ptr, PlanViewF *v);
+// re-bin a 2-D plan's nodes on tiles of edge T (8, 16 or 32)
+void plan_retile_f(void *nfftf_plan_ptr, int T);
+
 // ---------------------------------------------------------------- NDFT
 template <typename R>
 void launch_ndft_trafo(const R *x, const typename Cx<R>::T *fhat, typename Cx<R>::T *f,

@@ -91,6 +91,7 @@ struct Ctx {
   WorkItem *items = nullptr;
   int nitems = 0;
   int ntiles = 1;
+  int force_T = 0;  // 2-D tile edge set by the batch autotuner (0 = automatic)
   bool nodes_ready = false;
   cudaEvent_t ev[7] = {};
   // optional per-call event ring for timing a sequence of device calls
@@ -143,6 +144,7 @@ static void choose_tiles(Ctx<R> *c)
       }
     }
     c->tiled = T > 0;
+    if (c->tiled && c->force_T > 0 && g.d == 2) T = c->force_T;  // chosen by the batch autotuner
   }
   if (!c->tiled) T = g.d == 1 ? 256 : (g.d == 2 ? 32 : 8);  // binning only, for locality
   // 3-D: sub-cell group kernels on 8^3 tiles where the grid allows
@@ -944,3 +946,43 @@ GB_PLAN_API(nfftf_, float, 4)
 
 }  // extern "C"
 
+
+namespace gb {
+
+bool plan_view_f(void *pp, PlanViewF *v)
+{
+  nfftf_plan *p = reinterpret_cast<nfftf_plan *>(pp);
+  Ctx<float> *c = ctx_of<float>(p);
+  v->g = c->g;
+  v->xs = c->xs;
+  v->perm = c->perm;
+  v->cphi = c->cphi;
+  v->items = c->items;
+  v->nitems = c->nitems;
+  v->fhat = c->fhat_dev;
+  v->f = c->f_dev;
+  v->tiled = c->tiled;
+  v->group3 = c->group3;
+  v->direct = c->direct;
+  v->ready = c->nodes_ready;
+  v->stream = c->stream;
+  return true;
+}
+
+void plan_retile_f(void *pp, int T)
+{
+  nfftf_plan *p = reinterpret_cast<nfftf_plan *>(pp);
+  Ctx<float> *c = ctx_of<float>(p);
+  if (c->g.d != 2 || c->direct) return;
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  c->force_T = T;
+  choose_tiles<float>(c);
+  GB_CUDA(cudaFree(c->tile_start));
+  GB_CUDA(cudaFree(c->items));
+  const size_t M = (size_t)std::max<long long>(c->g.M, 1);
+  dev_alloc<float>((void **)&c->tile_start, ((size_t)c->ntiles + 1) * sizeof(uint32_t));
+  dev_alloc<float>((void **)&c->items, ((size_t)c->ntiles + M / 1024 + 2) * sizeof(WorkItem));
+  nodes_from_device<float>(p, c);
+}
+
+}  // namespace gb

@@ -1,0 +1,63 @@
+"""Batched 2-D transforms: every plan's batched result equals its own
+single-plan nfftf_trafo / nfftf_adjoint (which the parity tests pin to the
+reference), in stream and CUDA-graph mode, before and after autotuning."""
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from nfft_gb300 import batch
+
+pytestmark = pytest.mark.gpu
+
+
+def _single_results(plans, data, seed):
+    refs = []
+    for k, (p, (N, m, M, x)) in enumerate(zip(plans, data)):
+        r = np.random.default_rng([seed, k, 1])
+        fh = (r.uniform(-1, 1, N[0] * N[1]) + 1j * r.uniform(-1, 1, N[0] * N[1])).astype(np.complex64)
+        f = (r.uniform(-1, 1, M) + 1j * r.uniform(-1, 1, M)).astype(np.complex64)
+        p.f_hat[:] = fh
+        p.trafo()
+        tf = p.f.copy()
+        p.f[:] = f
+        p.adjoint()
+        tfh = p.f_hat.copy()
+        p.f[:] = tf
+        p.adjoint()
+        tff = p.f_hat.copy()  # A^H A f_hat
+        refs.append((fh, f, tf, tfh, tff))
+    return refs
+
+
+@pytest.mark.parametrize("autotune", [False, True])
+def test_batch_matches_single_plans(gpulib, autotune):
+    plans, data = batch.random_plans(gpulib, 24, seed=3, sizes=(32, 64), mmin=300, mmax=5000)
+    refs = _single_results(plans, data, 3)
+    b = batch.Batch(gpulib, plans)
+    if autotune:
+        assert b.autotune(reps=2) >= 1
+        cfgs = {b.config(k) for k in range(len(plans))}
+        assert all(T in (8, 16, 32) and t in (1, 4, 16) for T, t in cfgs)
+    put, get = batch.device_io(gpulib)
+    for p, (fh, f, *_r) in zip(plans, refs):
+        put(p, "f_hat", fh)
+    b.run(what=1, mode=0)
+    for p, (N, m, M, x), (fh, f, tf, tfh, tff) in zip(plans, data, refs):
+        assert rel_l2(get(p, "f", M), tf) < 1e-5
+        put(p, "f", f)
+    b.run(what=2, mode=0)
+    for p, (N, m, M, x), (fh, f, tf, tfh, tff) in zip(plans, data, refs):
+        assert rel_l2(get(p, "f_hat", N[0] * N[1]), tfh) < 1e-5
+        put(p, "f_hat", fh)
+    # graph mode: trafo then adjoint of its result, A^H A f_hat
+    b.run(what=3, mode=1)
+    for p, (N, m, M, x), (fh, f, tf, tfh, tff) in zip(plans, data, refs):
+        assert rel_l2(get(p, "f_hat", N[0] * N[1]), tff) < 1e-5
+        put(p, "f_hat", fh)
+    b.run(what=3, mode=1)  # the replay gives the same
+    for p, (N, m, M, x), (fh, f, tf, tfh, tff) in zip(plans, data, refs):
+        assert rel_l2(get(p, "f_hat", N[0] * N[1]), tff) < 1e-5
+    assert b.nodes == sum(d[2] for d in data)
+    b.close()
+    for p in plans:
+        p.finalize()

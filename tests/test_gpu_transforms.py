@@ -187,6 +187,31 @@ def test_online_vs_oracle(gpulib, N, M, m, single):
     assert rel_l2(gfh, rfh) < tol, rel_l2(gfh, rfh)
 
 
+@pytest.mark.parametrize("N,n,m,single", [
+    ([16, 16], [34, 34], 6, False),      # tile edge does not divide n; padded tile wraps twice
+    ([30, 20], [40, 44], 4, True),
+    ([6, 6, 6], [12, 12, 12], 4, True),  # 3-D sub-cell kernels on a grid smaller than tile + window
+    ([10, 12, 8], [20, 26, 18], 4, True),
+])
+def test_non_power_of_two_grids(gpulib, N, n, m, single):
+    M = 3000
+    x, fh, f = seeded_case(N, M, seed=13)
+    p = make_plan(gpulib, single, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    gf, gfh = run_both(p, x, fh, f)
+    idx = p.index_x
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m, single=single)
+    o.set_nodes(x.astype(np.float32) if single else x)
+    o.precompute()
+    assert np.array_equal(idx, o.index_x())
+    od = oracle.OraclePlan(N, M, n=n, m=m, single=False)
+    od.set_nodes(x.astype(np.float32).astype(np.float64) if single else x)
+    od.precompute()
+    tol = 2e-5 if single else 1e-12
+    assert rel_l2(gf, od.trafo(fh.astype(np.complex64) if single else fh)) < tol
+    assert rel_l2(gfh, od.adjoint(f.astype(np.complex64) if single else f)) < tol
+
+
 def test_clustered_nodes_and_heavy_tiles(gpulib):
     """Nodes packed into a few tiles: many work items per tile, same results."""
     rng = np.random.default_rng(5)

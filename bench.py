@@ -328,7 +328,7 @@ def run_gpu(args, wl):
     sums = (C.c_float * 7)()
     counts = (C.c_int * 2)()
     end(pa, sums, counts)
-    launches = 4 * args.steps  # d_pad + b_tiled (trafo), bt_tiled + d_crop (adjoint)
+    launches = 4 * args.steps  # k_d_pad + k_b3_group (trafo), k_bt3_group + k_d_crop (adjoint)
     if dist is not None:
         t = torch.tensor([ms_total], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -367,7 +367,8 @@ def run_gpu(args, wl):
              "adjoint_memset_ms": sums[3] / nA, "adjoint_BT_ms": sums[4] / nA,
              "adjoint_FFT_ms": sums[5] / nA, "adjoint_DT_ms": sums[6] / nA}
     b_ms, bt_ms = stage["trafo_B_ms"], stage["adjoint_BT_ms"]
-    dom, dom_ms = ("bt_tiled (B^T spreading)", bt_ms) if bt_ms >= b_ms else ("b_tiled (B interpolation)", b_ms)
+    kb, kbt = ("k_b3_group", "k_bt3_group") if wl["d"] == 3 else ("k_b_tiled", "k_bt_tiled")
+    dom, dom_ms = (kbt + " (B^T spreading)", bt_ms) if bt_ms >= b_ms else (kb + " (B interpolation)", b_ms)
     peaks, peak_kind = measured_peaks()
     bytes_b = algorithmic_bytes_B(wl)
     achieved = bytes_b / (dom_ms * 1e-3) / 1e9
@@ -375,7 +376,7 @@ def run_gpu(args, wl):
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
-        key = ("bt_tiled" if bt_ms >= b_ms else "b_tiled") + "/" + wl["dist"]
+        key = (kbt if bt_ms >= b_ms else kb) + "/" + wl["dist"]
         traffic = tr.get(key)
     except Exception:
         pass
@@ -469,6 +470,95 @@ def run_infft(args):
     return 0
 
 
+def run_batched(args):
+    """1024 independent 2-D complex64 plans: N_t log-uniform over {32..256},
+    sigma = 2, m in {4, 6}, M log-uniform in [1024, 65536], uniform nodes.
+    value = all plans' nodes per (trafo + adjoint of every plan) / time, with
+    the autotuned batch replayed as one CUDA graph; also reported: the same
+    batch as stream launches, before autotuning, and the plans one at a time
+    through their own device transforms."""
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import batch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lib = nfft_gb300.lib()
+    t0 = time.perf_counter()
+    plans, data = batch.random_plans(lib, args.plans, seed=0)
+    t_setup = time.perf_counter() - t0
+    nodes = sum(d[2] for d in data)
+    put, _ = batch.device_io(lib)
+    rng = np.random.default_rng(5)
+    for p, (N, m, M, x) in zip(plans, data):
+        put(p, "f_hat", (rng.uniform(-1, 1, N[0] * N[1]) + 1j * rng.uniform(-1, 1, N[0] * N[1])))
+    # one plan at a time (each plan's own D / cuFFT / B launches, no host sync in between)
+    tr = lib.nfftf_gb_trafo_device
+    ad = lib.nfftf_gb_adjoint_device
+    tr.argtypes = ad.argtypes = [C.c_void_p]
+    addrs = [C.addressof(p.p) for p in plans]
+    for a in addrs[:8]:
+        tr(a)
+        ad(a)
+    torch.cuda.synchronize()
+    reps = args.steps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for a in addrs:
+            tr(a)
+            ad(a)
+    torch.cuda.synchronize()
+    t_seq = (time.perf_counter() - t0) / reps
+    b = batch.Batch(lib, plans)
+    b.time(args.warmup, 0)
+    ms_stream_untuned = b.time(reps, 0)
+    ms_graph_untuned = b.time(reps, 1)
+    t0 = time.perf_counter()
+    classes = b.autotune(reps=3)
+    t_tune = time.perf_counter() - t0
+    b.time(args.warmup, 1)
+    ms_stream = b.time(reps, 0)
+    ms_graph = b.time(reps, 1)
+    cfgs = {}
+    for k in range(len(plans)):
+        cfgs.setdefault("%s" % (b.config(k),), 0)
+        cfgs["%s" % (b.config(k),)] += 1
+    line = {"metric": "nodes/s fwd+adj, batched uneven 2-D plans (one persistent graph-captured launch)",
+            "value": nodes / (ms_graph * 1e-3), "unit": "nodes/s", "n_gpus": 1, "steps": reps,
+            "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "%d 2-D complex64 plans, N_t in {32..256}, m in {4,6}, M in [1024,65536]"
+                       % len(plans), "nodes": nodes, "work_items": b.items},
+            "ms_per_round": {"graph_autotuned": ms_graph, "stream_autotuned": ms_stream,
+                             "graph_untuned": ms_graph_untuned, "stream_untuned": ms_stream_untuned,
+                             "one_plan_at_a_time_own_streams": t_seq * 1e3},
+            "speedup_vs_one_at_a_time": t_seq * 1e3 / ms_graph,
+            "autotune": {"classes": classes, "seconds": t_tune, "chosen_T_tpn_counts": cfgs},
+            "setup_s": t_setup}
+    b.close()
+    # the same plans one after another on one stream
+    ss = lib.nfftf_gb_set_stream
+    ss.argtypes = [C.c_void_p, C.c_void_p]
+    s = torch.cuda.Stream()
+    for a in addrs:
+        ss(a, C.c_void_p(s.cuda_stream))
+    for a in addrs[:8]:
+        tr(a)
+        ad(a)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for a in addrs:
+            tr(a)
+            ad(a)
+    torch.cuda.synchronize()
+    line["ms_per_round"]["one_plan_at_a_time_one_stream"] = (time.perf_counter() - t0) / reps * 1e3
+    for a in addrs:
+        ss(a, None)
+    for p in plans:
+        p.finalize()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned(args):
     """Learned density-compensation weights on 2-D spirals: N = 256^2, m = 6,
     16 interleaved Archimedean arms x 8192 samples (r = t/2, angle
@@ -554,7 +644,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
-                    choices=["uniform", "clustered", "small", "infft", "learned"])
+                    choices=["uniform", "clustered", "small", "infft", "learned", "batched"])
+    ap.add_argument("--plans", type=int, default=1024, help="plans of the batched workload")
     ap.add_argument("--train", type=int, default=256, help="training trajectories (learned)")
     ap.add_argument("--test", type=int, default=8, help="held-out trajectories (learned)")
     ap.add_argument("--epochs", type=int, default=3, help="training epochs (learned)")
@@ -569,7 +660,9 @@ def main():
         return run_infft(args)
     if args.workload == "learned":
         return run_learned(args)
-    wl = workload(args.workload)
+    if args.workload == "batched":
+        return run_batched(args)
+    wl =workload(args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_gpu(args, wl)

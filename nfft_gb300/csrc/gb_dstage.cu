@@ -39,66 +39,142 @@ void launch_cphi(const Geom<R> &g, double *cphi, cudaStream_t s)
   GB_LAUNCHED("cphi");
 }
 
-// One thread per grid cell, last dimension fastest: g = f_hat(k) prod_t c_t
-// inside the frequency box, zero elsewhere.
+// Row-wise D and D^T.  A block owns (part of) one grid row along the last
+// dimension: the row's position in the other dimensions, whether it meets
+// the frequency box and the product of their FP64 coefficients are computed
+// once per block with 32-bit index arithmetic; threads then stride along the
+// row with coalesced loads and stores.  In single precision the FP64
+// coefficient product is rounded once to float and applied in float.
 template <typename R>
-__global__ void k_d_pad(const typename Cx<R>::T *__restrict__ fhat, const double *__restrict__ cphi,
-                        typename Cx<R>::T *__restrict__ grid, Geom<R> g)
+__device__ __forceinline__ typename Cx<R>::T d_scale(typename Cx<R>::T v, double c);
+template <>
+__device__ __forceinline__ float2 d_scale<float>(float2 v, double c)
 {
-  typedef typename Cx<R>::T C;
-  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= g.n_total) return;
-  long long rem = cell;
-  long long fidx = 0;
-  double c = 1.0;
-  bool inside = true;
-  int off = 0;
-  int pos[GB_MAXD];
-  for (int t = g.d - 1; t >= 0; --t) {
-    pos[t] = (int)(rem % g.n[t]);
-    rem /= g.n[t];
-  }
-  for (int t = 0; t < g.d; ++t) {
-    const int i = pos[t];
-    const int k = (i < g.n[t] / 2) ? i : i - g.n[t];  // frequency at this grid point
-    const int kk = k + g.N[t] / 2;                     // natural-order index
-    if (kk < 0 || kk >= g.N[t]) inside = false;
-    else c *= cphi[off + kk];
-    fidx = fidx * g.N[t] + kk;
-    off += g.N[t];
-  }
-  C out = cmake(R(0), R(0));
-  if (inside) {
-    const C v = fhat[fidx];
-    out = cmake((R)((double)v.x * c), (R)((double)v.y * c));
-  }
-  grid[cell] = out;
+  const float cf = (float)c;
+  return make_float2(v.x * cf, v.y * cf);
+}
+template <>
+__device__ __forceinline__ double2 d_scale<double>(double2 v, double c)
+{
+  return make_double2(v.x * c, v.y * c);
 }
 
+// Natural-order index kk of grid position i (FFT order) along a dimension of
+// length n with bandwidth N, or -1 outside the frequency box.
+__device__ __forceinline__ int d_natural(int i, int n, int N)
+{
+  const int k = (i < n / 2) ? i : i - n;
+  const int kk = k + N / 2;
+  return (kk >= 0 && kk < N) ? kk : -1;
+}
+
+// Grid row r (over dims 0..d-2 of n) -> whether it meets the frequency box,
+// the natural-order row of f_hat it holds and the FP64 coefficient product.
 template <typename R>
-__global__ void k_d_crop(const typename Cx<R>::T *__restrict__ grid, const double *__restrict__ cphi,
-                         typename Cx<R>::T *__restrict__ fhat, Geom<R> g)
+__device__ __forceinline__ bool d_pad_row(unsigned r, const Geom<R> &g, const double *cphi, long long &frow,
+                                          double &c)
+{
+  bool inside = true;
+  long long fmul = 1;
+  int off = 0;
+  for (int t = 0; t < g.d - 1; ++t) off += g.N[t];
+  frow = 0;
+  c = 1.0;
+  for (int t = g.d - 2; t >= 0; --t) {
+    const unsigned nt = (unsigned)g.n[t];
+    const unsigned q = r / nt;
+    const int i = (int)(r - q * nt);
+    r = q;
+    off -= g.N[t];
+    const int kk = d_natural(i, g.n[t], g.N[t]);
+    if (kk < 0) inside = false;
+    else c *= cphi[off + kk];
+    frow += fmul * kk;
+    fmul *= g.N[t];
+  }
+  return inside;
+}
+
+// Row r of f_hat (over dims 0..d-2 of N) -> the grid row holding it and the
+// FP64 coefficient product.
+template <typename R>
+__device__ __forceinline__ long long d_crop_row(unsigned r, const Geom<R> &g, const double *cphi, double &c)
+{
+  long long grow = 0, gmul = 1;
+  int off = 0;
+  for (int t = 0; t < g.d - 1; ++t) off += g.N[t];
+  c = 1.0;
+  for (int t = g.d - 2; t >= 0; --t) {
+    const unsigned Nt = (unsigned)g.N[t];
+    const unsigned q = r / Nt;
+    const int kk = (int)(r - q * Nt);
+    r = q;
+    off -= g.N[t];
+    const int k = kk - g.N[t] / 2;
+    c *= cphi[off + kk];
+    grow += gmul * (k < 0 ? k + g.n[t] : k);
+    gmul *= g.n[t];
+  }
+  return grow;
+}
+
+// Trafo: g = f_hat(k) prod_t c_t inside the frequency box, zero elsewhere;
+// writes the whole n_total grid (no separate memset).  Blocks stride over
+// the grid rows.
+template <typename R>
+__global__ void __launch_bounds__(256) k_d_pad(const typename Cx<R>::T *__restrict__ fhat,
+                                               const double *__restrict__ cphi,
+                                               typename Cx<R>::T *__restrict__ grid, Geom<R> g)
 {
   typedef typename Cx<R>::T C;
-  const long long kl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (kl >= g.N_total) return;
-  long long rem = kl, gidx = 0;
-  double c = 1.0;
-  int kk[GB_MAXD];
-  for (int t = g.d - 1; t >= 0; --t) {
-    kk[t] = (int)(rem % g.N[t]);
-    rem /= g.N[t];
+  const int nl = g.n[g.d - 1], Nl = g.N[g.d - 1];
+  const double *cl = cphi;
+  for (int t = 0; t < g.d - 1; ++t) cl += g.N[t];
+  const unsigned rows = (unsigned)(g.n_total / nl);
+  for (unsigned r = blockIdx.x; r < rows; r += gridDim.x) {
+    long long frow;
+    double c;
+    const bool inside = d_pad_row<R>(r, g, cphi, frow, c);
+    C *row = grid + (long long)r * nl;
+    const C *src = fhat + frow * Nl;
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < nl; i += gridDim.y * blockDim.x) {
+      C out = cmake(R(0), R(0));
+      const int kk = d_natural(i, nl, Nl);
+      if (inside && kk >= 0) out = d_scale<R>(src[kk], c * cl[kk]);
+      row[i] = out;
+    }
   }
-  int off = 0;
-  for (int t = 0; t < g.d; ++t) {
-    const int k = kk[t] - g.N[t] / 2;
-    const int i = k < 0 ? k + g.n[t] : k;
-    gidx = gidx * g.n[t] + i;
-    c *= cphi[off + kk[t]];
-    off += g.N[t];
+}
+
+// Adjoint: f_hat(k) = g(k mod n) prod_t c_t.  Blocks stride over the rows
+// of f_hat.
+template <typename R>
+__global__ void __launch_bounds__(256) k_d_crop(const typename Cx<R>::T *__restrict__ grid,
+                                                const double *__restrict__ cphi,
+                                                typename Cx<R>::T *__restrict__ fhat, Geom<R> g)
+{
+  typedef typename Cx<R>::T C;
+  const int nl = g.n[g.d - 1], Nl = g.N[g.d - 1];
+  const double *cl = cphi;
+  for (int t = 0; t < g.d - 1; ++t) cl += g.N[t];
+  const unsigned rows = (unsigned)(g.N_total / Nl);
+  for (unsigned r = blockIdx.x; r < rows; r += gridDim.x) {
+    double c;
+    const C *src = grid + d_crop_row<R>(r, g, cphi, c) * nl;
+    C *out = fhat + (long long)r * Nl;
+    for (int kk = blockIdx.y * blockDim.x + threadIdx.x; kk < Nl; kk += gridDim.y * blockDim.x) {
+      const int k = kk - Nl / 2;
+      out[kk] = d_scale<R>(src[k < 0 ? k + nl : k], c * cl[kk]);
+    }
   }
-  const C v = grid[gidx];
-  fhat[kl] = cmake((R)((double)v.x * c), (R)((double)v.y * c));
+}
+
+// blocks stride over rows (at most 16 resident blocks' worth per SM)
+static dim3 d_rows_grid(long long rows, int len, int th)
+{
+  const long long chunks = (len + th - 1) / th;
+  const long long bx = rows < 152 * 16 ? rows : 152 * 16;
+  return dim3((unsigned)bx, (unsigned)(chunks < 65535 ? chunks : 65535), 1);
 }
 
 template <typename R>
@@ -106,7 +182,8 @@ void launch_d_pad(const typename Cx<R>::T *fhat, const double *cphi, typename Cx
                   const Geom<R> &g, cudaStream_t s)
 {
   const int th = 256;
-  k_d_pad<R><<<(unsigned)((g.n_total + th - 1) / th), th, 0, s>>>(fhat, cphi, grid, g);
+  const int nl = g.n[g.d - 1];
+  k_d_pad<R><<<d_rows_grid(g.n_total / nl, nl, th), th, 0, s>>>(fhat, cphi, grid, g);
   GB_LAUNCHED("d_pad");
 }
 
@@ -115,7 +192,8 @@ void launch_d_crop(const typename Cx<R>::T *grid, const double *cphi, typename C
                    const Geom<R> &g, cudaStream_t s)
 {
   const int th = 256;
-  k_d_crop<R><<<(unsigned)((g.N_total + th - 1) / th), th, 0, s>>>(grid, cphi, fhat, g);
+  const int Nl = g.N[g.d - 1];
+  k_d_crop<R><<<d_rows_grid(g.N_total / Nl, Nl, th), th, 0, s>>>(grid, cphi, fhat, g);
   GB_LAUNCHED("d_crop");
 }
 

@@ -14,7 +14,7 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
                    cudaStream_t s)
 {
   static bool attr = false;
-  const size_t smem = adjoint ? g3_smem_bytes<R, W, G3_CS, g3_pm_bt<R>()>(g) : g3_smem_bytes<R, W, G3_CS, g3_pm_b<R>()>(g);
+  const size_t smem = adjoint ? g3_smem_bytes<R, W, G3_CS, true>(g) : g3_smem_bytes<R, W, G3_CS, false>(g);
   if (!attr) {
     GB_CUDA(cudaFuncSetAttribute(k_b3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  200 * 1024));
@@ -37,9 +37,9 @@ template <> struct G3Set<float> {
   static size_t smem(const Geom<float> &g)
   {
     switch (g.w) {
-      case 8: return g3_smem_bytes<float, 8, G3_CS>(g);
-      case 10: return g3_smem_bytes<float, 10, G3_CS>(g);
-      case 14: return g3_smem_bytes<float, 14, G3_CS>(g);
+      case 8: return g3_smem_max<float, 8, G3_CS>(g);
+      case 10: return g3_smem_max<float, 10, G3_CS>(g);
+      case 14: return g3_smem_max<float, 14, G3_CS>(g);
     }
     return 0;
   }
@@ -59,8 +59,8 @@ template <> struct G3Set<double> {
   static size_t smem(const Geom<double> &g)
   {
     switch (g.w) {
-      case 10: return g3_smem_bytes<double, 10, G3_CS>(g);
-      case 14: return g3_smem_bytes<double, 14, G3_CS>(g);
+      case 10: return g3_smem_max<double, 10, G3_CS>(g);
+      case 14: return g3_smem_max<double, 14, G3_CS>(g);
     }
     return 0;
   }

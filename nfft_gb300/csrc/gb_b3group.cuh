@@ -35,49 +35,86 @@ namespace gb {
 static constexpr int G3_THREADS = 256;
 static constexpr int G3_WARPS = G3_THREADS / 32;
 static constexpr int G3_TILE = 8;          // tile edge (cells)
-static constexpr int G3_WINDOW = 1024;     // nodes per unit-building window
+// Nodes per unit-building window (B, B^T): a smaller window shrinks the
+// index scratch, which lets three B^T CTAs share an SM.
+#ifndef GB_G3_WINDOW
+#define GB_G3_WINDOW 1024
+#endif
+#ifndef GB_G3_WINDOW_BT
+#define GB_G3_WINDOW_BT 512
+#endif
 static constexpr int G3_MAXITEM = 16384;   // nodes per work item
 
-// nodes per unit: B keeps 2 PMAX partial sums per lane, B^T 2 (w + CS - 1)
-// accumulators, so B^T prefers smaller units
-template <typename R> __host__ __device__ constexpr int g3_pm_b() { return sizeof(R) == 4 ? 16 : 8; }
-template <typename R> __host__ __device__ constexpr int g3_pm_bt() { return 8; }
+// Nodes per unit: B keeps 2 PMAX partial sums per lane, B^T 2 (w + CS - 1)
+// accumulators per row, so B^T prefers smaller units.
+#ifndef GB_G3_PM_B_FLOAT
+#define GB_G3_PM_B_FLOAT 16
+#endif
+#ifndef GB_G3_PM_BT_FLOAT
+#define GB_G3_PM_BT_FLOAT 16
+#endif
+// Box rows a lane holds at once (they share the unit's z weight vectors);
+// B^T keeps 2 (w + CS - 1) accumulators per row, so it holds fewer.
+#ifndef GB_G3_ROWS_PER_LANE
+#define GB_G3_ROWS_PER_LANE 2
+#endif
+#ifndef GB_G3_ROWS_PER_LANE_BT
+#define GB_G3_ROWS_PER_LANE_BT 1
+#endif
+template <typename R> __host__ __device__ constexpr int g3_pm_b() { return sizeof(R) == 4 ? GB_G3_PM_B_FLOAT : 8; }
+template <typename R> __host__ __device__ constexpr int g3_pm_bt() { return sizeof(R) == 4 ? GB_G3_PM_BT_FLOAT : 8; }
+template <typename R, int W, bool ADJ> __host__ __device__ constexpr int g3_rpl()
+{
+  return (sizeof(R) == 4 && W >= 10 && W <= 12) ? (ADJ ? GB_G3_ROWS_PER_LANE_BT : GB_G3_ROWS_PER_LANE) : 1;
+}
 
-template <typename R, int W, int CS, int PM>
+template <typename R, int W, int CS, int PM, bool ADJ = false>
 struct G3 {
   static constexpr int EXT = G3_TILE + W - 1;                     // padded subgrid edge
   static constexpr int BOX = W + CS - 1;                          // box edge
   static constexpr int BOXP = (BOX + 3) / 4 * 4;                  // padded for vector loads
   static constexpr int ROWS = BOX * BOX;                          // (x, y) rows of a box
-  static constexpr int RITER = (ROWS + 31) / 32;                  // row iterations per lane
+  static constexpr int RPL = g3_rpl<R, W, ADJ>();                 // rows a lane holds at once
+  static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);  // row iterations per lane
   static constexpr int PMAX = PM;                                 // nodes per unit
   static constexpr int NV = 2 * PMAX;                             // reduced values per unit
-  // per-warp scratch (R): wx, wy, wz [PMAX][BOXP] each, f values [PMAX][2],
-  // window offsets t0 [3 PMAX], box offsets o [3 PMAX] (as int)
-  static constexpr int WARP_FLOATS = 3 * PMAX * BOXP + 2 * PMAX + 6 * PMAX;
-  static constexpr int INTS = 4 * G3_WINDOW + 2 + G3_WARPS;       // sub, gstart, ucount, ustart, wsum
+  // per-warp scratch (R): window vectors [4][PMAX][BOXP] (x, y, z, and for
+  // B^T x scaled by Im f while slot 0 holds x scaled by Re f)
+  static constexpr int WARP_FLOATS = 4 * PMAX * BOXP;
+  static constexpr int WIN = ADJ ? GB_G3_WINDOW_BT : GB_G3_WINDOW;  // nodes per unit-building window
+  static constexpr int INTS = 4 * WIN + 2 + G3_WARPS;             // sub, gstart, ucount, ustart, wsum
 };
 
-template <typename R, int W, int CS, int PM = (g3_pm_b<R>() > g3_pm_bt<R>() ? g3_pm_b<R>() : g3_pm_bt<R>())>
+template <typename R, int W, int CS, bool ADJ>
 inline size_t g3_smem_bytes(const Geom<R> &g)
 {
-  typedef G3<R, W, CS, PM> P;
+  typedef G3<R, W, CS, ADJ ? g3_pm_bt<R>() : g3_pm_b<R>(), ADJ> P;
   const size_t plane = (size_t)P::EXT * g.sx;
   return (2 * plane + (size_t)G3_WARPS * P::WARP_FLOATS) * sizeof(R) + P::INTS * sizeof(int);
 }
 
-// Butterfly transpose-reduction over the warp: NV values per lane in; lane l
-// holds the warp-wide sum of value (l mod NV) in v[0] on return.
-template <typename R, int NV>
+// the larger of the B and B^T kernels' dynamic shared memory
+template <typename R, int W, int CS>
+inline size_t g3_smem_max(const Geom<R> &g)
+{
+  const size_t b = g3_smem_bytes<R, W, CS, false>(g), bt = g3_smem_bytes<R, W, CS, true>(g);
+  return b > bt ? b : bt;
+}
+
+// Butterfly transpose-reduction over the warp of the first K (16 or 32)
+// values of each lane; lane l holds the warp-wide sum of value (l mod K) in
+// v[0] on return.
+template <typename R, int K, int NV>
 __device__ __forceinline__ void warp_transpose_reduce(R (&v)[NV])
 {
+  static_assert(K <= NV && (K == 16 || K == 32), "K");
   const int lane = threadIdx.x & 31;
-  if (NV == 16) {
+  if (K == 16) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], 16);
   }
 #pragma unroll
-  for (int h = NV / 2; h >= 1; h >>= 1) {
+  for (int h = K / 2; h >= 1; h >>= 1) {
     const bool upper = (lane & h) != 0;
 #pragma unroll
     for (int i = 0; i < h; ++i) {
@@ -187,13 +224,33 @@ __device__ int g3_units(int c0, int c1, const R *__restrict__ xs, const Geom<R> 
   return nu;
 }
 
-// All 32 lanes evaluate the window values of the unit's np nodes into the
-// warp's zero-padded box vectors w[t][j][b] ([3][PMAX][BOXP]).  t0 / so are
-// per (node, dim) scratch: t0 = n x - u (the argument of tap 0), so = box
-// offset of the window.
+// store BOXP reals (a padded window vector) to shared memory with vector stores
+template <typename R, int BOXP>
+__device__ __forceinline__ void g3_store_vec(R *dst, const R (&src)[BOXP])
+{
+  typedef typename std::conditional<sizeof(R) == 4, float4, double2>::type V;
+  constexpr int VPER = sizeof(V) / sizeof(R);
+  V *v = reinterpret_cast<V *>(dst);
+#pragma unroll
+  for (int q = 0; q < BOXP / VPER; ++q) {
+    V t;
+    R *tt = reinterpret_cast<R *>(&t);
+#pragma unroll
+    for (int e = 0; e < VPER; ++e) tt[e] = src[q * VPER + e];
+    v[q] = t;
+  }
+}
+
+// Window vectors of a unit: lane k < 3 np takes node j = k / 3, dimension
+// t = k mod 3, evaluates its W taps phi(t0 - l), t0 = n x - u, and stores
+// them zero-padded at the window's offset so in [0, CS) of the box:
+// w[t][j][b] ([3][PMAX][BOXP]).  With fv != nullptr (B^T), the x vector is
+// stored twice, scaled by Re f_j in slot 0 and by Im f_j in slot 3.
 template <typename R, int W, int CS, int PM>
 __device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restrict__ xs, const Geom<R> &g,
-                                                const int *org, const int *box0, R *w, R *t0, int *so)
+                                                const int *org, const int *box0, R *w,
+                                                const typename Cx<R>::T *__restrict__ fv = nullptr,
+                                                const uint32_t *__restrict__ perm = nullptr)
 {
   typedef G3<R, W, CS, PM> P;
   const int lane = threadIdx.x & 31;
@@ -201,17 +258,31 @@ __device__ __forceinline__ void g3_unit_weights(int u0, int np, const R *__restr
     const int j = k / 3, t = k - 3 * j;
     const R xn = xs[(long long)(u0 + j) * 3 + t] * g.nR[t];
     const int u = (int)gb_floor(xn) - g.m;  // node_u
-    so[k] = wrap(u, g.n[t]) - org[t] - box0[t];
-    t0[k] = xn - R(u);
-  }
-  __syncwarp();
-  for (int k = lane; k < 3 * np * P::BOXP; k += 32) {
-    const int jt = k / P::BOXP, b = k - jt * P::BOXP;
-    const int j = jt / 3, t = jt - 3 * j;
-    const int l = b - so[jt];
-    R v = R(0);
-    if (l >= 0 && l < W) v = kb_window_t(t0[jt] - R(l), g.mm, g.b[t]);
-    w[(t * P::PMAX + j) * P::BOXP + b] = v;
+    const int so = wrap(u, g.n[t]) - org[t] - box0[t];
+    const R t0 = xn - R(u);
+    R v[W];
+#pragma unroll
+    for (int l = 0; l < W; ++l) v[l] = kb_window_t(t0 - R(l), g.mm, g.b[t]);
+    R out[P::BOXP];
+#pragma unroll
+    for (int b = 0; b < P::BOXP; ++b) {
+      R val = R(0);
+#pragma unroll
+      for (int c = 0; c < CS; ++c)
+        if (b - c >= 0 && b - c < W && so == c) val = v[b - c];
+      out[b] = val;
+    }
+    if (fv != nullptr && t == 0) {
+      const typename Cx<R>::T fj = fv[perm[u0 + j]];
+      R o2[P::BOXP];
+#pragma unroll
+      for (int b = 0; b < P::BOXP; ++b) {
+        o2[b] = out[b] * fj.y;
+        out[b] *= fj.x;
+      }
+      g3_store_vec<R, P::BOXP>(w + (3 * P::PMAX + j) * P::BOXP, o2);
+    }
+    g3_store_vec<R, P::BOXP>(w + (t * P::PMAX + j) * P::BOXP, out);
   }
   __syncwarp();
 }
@@ -257,29 +328,114 @@ __device__ __forceinline__ void g3_load_vec(const R *src, R (&dst)[BOXP])
   }
 }
 
-template <typename R, int W, int CS, int PM>
+// z contraction of one box row (B): (tr, ti) = sum_z wz[z] (gr[z], gi[z]).
+template <typename R, int BOX, int BOXP>
+__device__ __forceinline__ void g3_zdot(const R (&wz)[BOXP], const R (&gr)[BOX], const R (&gi)[BOX], R &tr, R &ti)
+{
+  R r0 = R(0), i0 = R(0), r1 = R(0), i1 = R(0);
+#pragma unroll
+  for (int z = 0; z + 1 < BOX; z += 2) {
+    r0 += wz[z] * gr[z];
+    i0 += wz[z] * gi[z];
+    r1 += wz[z + 1] * gr[z + 1];
+    i1 += wz[z + 1] * gi[z + 1];
+  }
+  if (BOX & 1) {
+    r0 += wz[BOX - 1] * gr[BOX - 1];
+    i0 += wz[BOX - 1] * gi[BOX - 1];
+  }
+  tr = r0 + r1;
+  ti = i0 + i1;
+}
+
+// FP32: two adjacent z taps per paired FMA (fma.rn.f32x2 of the sm_100
+// family), halving the issued instructions of the dominant loop.
+template <int BOX, int BOXP>
+__device__ __forceinline__ void g3_zdot(const float (&wz)[BOXP], const float (&gr)[BOX], const float (&gi)[BOX],
+                                        float &tr, float &ti)
+{
+  float2 r2 = make_float2(0.f, 0.f), i2 = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int z = 0; z + 1 < BOX; z += 2) {
+    const float2 w2 = make_float2(wz[z], wz[z + 1]);
+    r2 = __ffma2_rn(w2, make_float2(gr[z], gr[z + 1]), r2);
+    i2 = __ffma2_rn(w2, make_float2(gi[z], gi[z + 1]), i2);
+  }
+  tr = r2.x + r2.y;
+  ti = i2.x + i2.y;
+  if (BOX & 1) {
+    tr += wz[BOX - 1] * gr[BOX - 1];
+    ti += wz[BOX - 1] * gi[BOX - 1];
+  }
+}
+
+// rank-1 update of one box row (B^T): (ar[z], ai[z]) += wz[z] (hr, hi).
+template <typename R, int BOX, int BOXP>
+__device__ __forceinline__ void g3_zaxpy(const R (&wz)[BOXP], R hr, R hi, R (&ar)[BOX], R (&ai)[BOX])
+{
+#pragma unroll
+  for (int z = 0; z < BOX; ++z) {
+    ar[z] += wz[z] * hr;
+    ai[z] += wz[z] * hi;
+  }
+}
+
+template <int BOX, int BOXP>
+__device__ __forceinline__ void g3_zaxpy(const float (&wz)[BOXP], float hr, float hi, float (&ar)[BOX],
+                                         float (&ai)[BOX])
+{
+  const float2 h2r = make_float2(hr, hr), h2i = make_float2(hi, hi);
+#pragma unroll
+  for (int z = 0; z + 1 < BOX; z += 2) {
+    const float2 w2 = make_float2(wz[z], wz[z + 1]);
+    const float2 a = __ffma2_rn(w2, h2r, make_float2(ar[z], ar[z + 1]));
+    const float2 b = __ffma2_rn(w2, h2i, make_float2(ai[z], ai[z + 1]));
+    ar[z] = a.x;
+    ar[z + 1] = a.y;
+    ai[z] = b.x;
+    ai[z + 1] = b.y;
+  }
+  if (BOX & 1) {
+    ar[BOX - 1] += wz[BOX - 1] * hr;
+    ai[BOX - 1] += wz[BOX - 1] * hi;
+  }
+}
+
+template <typename R, int W, int CS, int PM, bool ADJ>
 struct G3Smem {
-  R *w, *fv, *t0;
-  int *so;
+  R *w;
   R *sre, *sim;
   int *sub, *gstart, *ucnt, *ustart, *wsum;
   __device__ G3Smem(unsigned char *raw, const Geom<R> &g)
   {
-    typedef G3<R, W, CS, PM> P;
+    typedef G3<R, W, CS, PM, ADJ> P;
     R *base = reinterpret_cast<R *>(raw);  // per-warp scratch first: 16-byte aligned
     w = base + (threadIdx.x >> 5) * P::WARP_FLOATS;
-    fv = w + 3 * P::PMAX * P::BOXP;
-    t0 = fv + 2 * P::PMAX;
-    so = reinterpret_cast<int *>(t0 + 3 * P::PMAX);
     sre = base + G3_WARPS * P::WARP_FLOATS;
     sim = sre + P::EXT * g.sx;
     sub = reinterpret_cast<int *>(sim + P::EXT * g.sx);
-    gstart = sub + G3_WINDOW;
-    ucnt = gstart + G3_WINDOW + 1;
-    ustart = ucnt + G3_WINDOW;
-    wsum = ustart + G3_WINDOW + 1;
+    gstart = sub + P::WIN;
+    ucnt = gstart + P::WIN + 1;
+    ustart = ucnt + P::WIN;
+    wsum = ustart + P::WIN + 1;
   }
 };
+
+// The box rows a lane holds in row iteration ri: row = lane + 32 (ri RPL + q);
+// rows past the box are clamped to row 0 and flagged.
+template <typename P>
+__device__ __forceinline__ void g3_rows(int ri, int lane, int (&bx)[P::RPL], int (&by)[P::RPL],
+                                        bool (&ok)[P::RPL])
+{
+#pragma unroll
+  for (int q = 0; q < P::RPL; ++q) {
+    const int row = lane + 32 * (ri * P::RPL + q);
+    ok[q] = row < P::ROWS;
+    const int rr = ok[q] ? row : 0;
+    bx[q] = rr / P::BOX;
+    by[q] = rr - bx[q] * P::BOX;
+  }
+}
 
 template <typename R, int W, int CS>
 __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__restrict__ items,
@@ -290,15 +446,18 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
 {
   constexpr int PM = g3_pm_b<R>();
   typedef G3<R, W, CS, PM> P;
+  constexpr int RPL = P::RPL;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  G3Smem<R, W, CS, PM> S(smem_raw, g);
+  G3Smem<R, W, CS, PM, false> S(smem_raw, g);
   const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
   g3_tile_origin<R>(it, g, org);
+  // several grid loads in flight per thread
+#pragma unroll 4
   for (int idx = threadIdx.x; idx < P::EXT * P::EXT * P::EXT; idx += G3_THREADS) {
     int si;
     long long gi;
@@ -307,55 +466,56 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_b3_group(const WorkItem *__re
     S.sre[si] = v.x;
     S.sim[si] = v.y;
   }
-  for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
-    const int c1 = min(c0 + G3_WINDOW, it.end);
+  for (int c0 = it.start; c0 < it.end; c0 += P::WIN) {
+    const int c1 = min(c0 + P::WIN, it.end);
     const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, S.sub, S.gstart, S.ucnt, S.ustart, S.wsum);
     for (int ui = warp; ui < nu; ui += G3_WARPS) {
       const int u0 = S.ustart[ui], np = S.ustart[ui + 1] - u0;
       int box0[3];
       node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
-      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);
+      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w);
       const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
       R acc[P::NV];
 #pragma unroll
       for (int j = 0; j < P::NV; ++j) acc[j] = R(0);
 #pragma unroll 1
       for (int ri = 0; ri < P::RITER; ++ri) {
-        const int row = lane + 32 * ri;
-        if (row < P::ROWS) {
-          const int bx = row / P::BOX, by = row - bx * P::BOX;
-          const int base = sbase + bx * g.sx + by * g.sy;
-          R gr[P::BOX], gim[P::BOX];
+        int bx[RPL], by[RPL];
+        bool ok[RPL];
+        g3_rows<P>(ri, lane, bx, by, ok);
+        R gr[RPL][P::BOX], gim[RPL][P::BOX];
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+          const int base = sbase + bx[q] * g.sx + by[q] * g.sy;
 #pragma unroll
           for (int z = 0; z < P::BOX; ++z) {
-            gr[z] = S.sre[base + z];
-            gim[z] = S.sim[base + z];
+            gr[q][z] = S.sre[base + z];
+            gim[q][z] = S.sim[base + z];
           }
+        }
 #pragma unroll
-          for (int j = 0; j < P::PMAX; ++j) {
-            if (j < np) {
-              R wzj[P::BOXP];
-              g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
-              R tr0 = R(0), ti0 = R(0), tr1 = R(0), ti1 = R(0);
+        for (int j = 0; j < P::PMAX; ++j) {
+          if (j < np) {
+            R wzj[P::BOXP];
+            g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
+            R tr[RPL], ti[RPL];
 #pragma unroll
-              for (int z = 0; z + 1 < P::BOX; z += 2) {
-                tr0 += wzj[z] * gr[z];
-                ti0 += wzj[z] * gim[z];
-                tr1 += wzj[z + 1] * gr[z + 1];
-                ti1 += wzj[z + 1] * gim[z + 1];
-              }
-              if (P::BOX & 1) {
-                tr0 += wzj[P::BOX - 1] * gr[P::BOX - 1];
-                ti0 += wzj[P::BOX - 1] * gim[P::BOX - 1];
-              }
-              const R wxy = wx[j * P::BOXP + bx] * wy[j * P::BOXP + by];
-              acc[2 * j] += wxy * (tr0 + tr1);
-              acc[2 * j + 1] += wxy * (ti0 + ti1);
+            for (int q = 0; q < RPL; ++q) g3_zdot(wzj, gr[q], gim[q], tr[q], ti[q]);
+#pragma unroll
+            for (int q = 0; q < RPL; ++q) {
+              const R wxy = ok[q] ? wx[j * P::BOXP + bx[q]] * wy[j * P::BOXP + by[q]] : R(0);
+              acc[2 * j] += wxy * tr[q];
+              acc[2 * j + 1] += wxy * ti[q];
             }
           }
         }
       }
-      warp_transpose_reduce<R, P::NV>(acc);
+      if constexpr (P::NV >= 32) {
+        if (np > 8) warp_transpose_reduce<R, 32>(acc);
+        else warp_transpose_reduce<R, 16>(acc);
+      } else {
+        warp_transpose_reduce<R, 16>(acc);
+      }
       const R re = __shfl_sync(0xffffffffu, acc[0], (2 * lane) & 31);
       const R im = __shfl_sync(0xffffffffu, acc[0], (2 * lane + 1) & 31);
       if (lane < np) f[perm[u0 + lane]] = cmake(re, im);
@@ -374,12 +534,15 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
                                                               Geom<R> g)
 {
   constexpr int PM = g3_pm_bt<R>();
-  typedef G3<R, W, CS, PM> P;
+  typedef G3<R, W, CS, PM, true> P;
+  constexpr int RPL = P::RPL;
   typedef typename Cx<R>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  G3Smem<R, W, CS, PM> S(smem_raw, g);
-  const R *wx = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
+  G3Smem<R, W, CS, PM, true> S(smem_raw, g);
+  // x vectors scaled by Re f (slot 0) and Im f (slot 3), y, z
+  const R *wxr = S.w, *wy = S.w + P::PMAX * P::BOXP, *wz = S.w + 2 * P::PMAX * P::BOXP;
+  const R *wxi = S.w + 3 * P::PMAX * P::BOXP;
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
@@ -388,47 +551,50 @@ __global__ void __launch_bounds__(G3_THREADS, 2) k_bt3_group(const WorkItem *__r
     S.sre[i] = R(0);
     S.sim[i] = R(0);
   }
-  for (int c0 = it.start; c0 < it.end; c0 += G3_WINDOW) {
-    const int c1 = min(c0 + G3_WINDOW, it.end);
+  for (int c0 = it.start; c0 < it.end; c0 += P::WIN) {
+    const int c1 = min(c0 + P::WIN, it.end);
     const int nu = g3_units<R, CS, P::PMAX>(c0, c1, xs, g, org, S.sub, S.gstart, S.ucnt, S.ustart, S.wsum);
     for (int ui = warp; ui < nu; ui += G3_WARPS) {
       const int u0 = S.ustart[ui], np = S.ustart[ui + 1] - u0;
       int box0[3];
       node_subcell<R, CS>(xs + (long long)u0 * 3, g, org, box0);
-      if (lane < np) {
-        const C v = f[perm[u0 + lane]];
-        S.fv[2 * lane] = v.x;
-        S.fv[2 * lane + 1] = v.y;
-      }
-      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w, S.t0, S.so);  // ends with __syncwarp
+      g3_unit_weights<R, W, CS, PM>(u0, np, xs, g, org, box0, S.w, f, perm);  // ends with __syncwarp
       const int sbase = box0[0] * g.sx + box0[1] * g.sy + box0[2];
 #pragma unroll 1
       for (int ri = 0; ri < P::RITER; ++ri) {
-        const int row = lane + 32 * ri;
-        if (row < P::ROWS) {
-          const int bx = row / P::BOX, by = row - bx * P::BOX;
-          R ar[P::BOX], ai[P::BOX];
+        int bx[RPL], by[RPL];
+        bool ok[RPL];
+        g3_rows<P>(ri, lane, bx, by, ok);
+        R ar[RPL][P::BOX], ai[RPL][P::BOX];
 #pragma unroll
-          for (int z = 0; z < P::BOX; ++z) ar[z] = ai[z] = R(0);
+        for (int q = 0; q < RPL; ++q)
 #pragma unroll
-          for (int j = 0; j < P::PMAX; ++j) {
-            if (j < np) {
-              const R wxy = wx[j * P::BOXP + bx] * wy[j * P::BOXP + by];
-              const R hr = wxy * S.fv[2 * j], hi = wxy * S.fv[2 * j + 1];
-              R wzj[P::BOXP];
-              g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
+          for (int z = 0; z < P::BOX; ++z) ar[q][z] = ai[q][z] = R(0);
 #pragma unroll
-              for (int z = 0; z < P::BOX; ++z) {
-                ar[z] += wzj[z] * hr;
-                ai[z] += wzj[z] * hi;
-              }
+        for (int j = 0; j < P::PMAX; ++j) {
+          if (j < np) {
+            R hr[RPL], hi[RPL];
+#pragma unroll
+            for (int q = 0; q < RPL; ++q) {
+              const R wyq = wy[j * P::BOXP + by[q]];
+              hr[q] = wxr[j * P::BOXP + bx[q]] * wyq;
+              hi[q] = wxi[j * P::BOXP + bx[q]] * wyq;
             }
-          }
-          const int base = sbase + bx * g.sx + by * g.sy;
+            R wzj[P::BOXP];
+            g3_load_vec<R, P::BOXP>(wz + j * P::BOXP, wzj);
 #pragma unroll
-          for (int z = 0; z < P::BOX; ++z) {
-            atomicAdd(S.sre + base + z, ar[z]);
-            atomicAdd(S.sim + base + z, ai[z]);
+            for (int q = 0; q < RPL; ++q) g3_zaxpy(wzj, hr[q], hi[q], ar[q], ai[q]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+          if (ok[q]) {
+            const int base = sbase + bx[q] * g.sx + by[q] * g.sy;
+#pragma unroll
+            for (int z = 0; z < P::BOX; ++z) {
+              atomicAdd(S.sre + base + z, ar[q][z]);
+              atomicAdd(S.sim + base + z, ai[q][z]);
+            }
           }
         }
       }

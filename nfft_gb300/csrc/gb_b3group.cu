@@ -1,8 +1,10 @@
 // gb_b3group.cu -- instantiations and launchers of the 3-D sub-cell group
 // kernels (see gb_b3group.cuh).
+#include <algorithm>
 #include <type_traits>
 
 #include "gb_b3group.cuh"
+#include "gb_col3.cuh"
 
 namespace gb {
 
@@ -11,8 +13,29 @@ static constexpr int G3_CS = 2;  // sub-cell edge
 template <typename R, int W>
 static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<R>::T *grid,
                    const R *xs, const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g,
-                   cudaStream_t s)
+                   const WinPoly &poly, cudaStream_t s)
 {
+  (void)poly;
+  if constexpr (std::is_same<R, float>::value && W == 10) {
+    if (adjoint) {
+      static bool attr_col = false;
+      if (!attr_col) {
+        GB_CUDA(cudaFuncSetAttribute(k_bt3_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_col = true;
+      }
+      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, xs, perm, f, g, poly);
+      GB_LAUNCHED("bt3_col");
+      return;
+    }
+    static bool attr_cell = false;
+    if (!attr_cell) {
+      GB_CUDA(cudaFuncSetAttribute(k_b3_cell<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr_cell = true;
+    }
+    k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, xs, perm, f, g, poly);
+    GB_LAUNCHED("b3_cell");
+    return;
+  }
   static bool attr = false;
   const size_t smem = adjoint ? g3_smem_bytes<R, W, G3_CS, true>(g) : g3_smem_bytes<R, W, G3_CS, false>(g);
   if (!attr) {
@@ -38,24 +61,26 @@ template <> struct G3Set<float> {
   {
     switch (g.w) {
       case 8: return g3_smem_max<float, 8, G3_CS>(g);
-      case 10: return g3_smem_max<float, 10, G3_CS>(g);
+      case 10: return std::max({g3_smem_max<float, 10, G3_CS>(g), c3_smem_bytes<10>(g), s3_smem_bytes<10>(g)});
       case 14: return g3_smem_max<float, 14, G3_CS>(g);
     }
     return 0;
   }
+  static bool column(int w) { return w == 10; }
   static void run(bool adj, const WorkItem *it, int ni, float2 *grid, const float *xs, const uint32_t *perm,
-                  float2 *f, const Geom<float> &g, cudaStream_t s)
+                  float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
   {
     switch (g.w) {
-      case 8: run_g3<float, 8>(adj, it, ni, grid, xs, perm, f, g, s); return;
-      case 10: run_g3<float, 10>(adj, it, ni, grid, xs, perm, f, g, s); return;
-      case 14: run_g3<float, 14>(adj, it, ni, grid, xs, perm, f, g, s); return;
+      case 8: run_g3<float, 8>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
+      case 10: run_g3<float, 10>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
+      case 14: run_g3<float, 14>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
     }
     fatal("no 3-D group kernel for w=%d", g.w);
   }
 };
 template <> struct G3Set<double> {
   static bool has(int w) { return w == 10 || w == 14; }
+  static bool column(int) { return false; }
   static size_t smem(const Geom<double> &g)
   {
     switch (g.w) {
@@ -65,11 +90,11 @@ template <> struct G3Set<double> {
     return 0;
   }
   static void run(bool adj, const WorkItem *it, int ni, double2 *grid, const double *xs,
-                  const uint32_t *perm, double2 *f, const Geom<double> &g, cudaStream_t s)
+                  const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPoly &poly, cudaStream_t s)
   {
     switch (g.w) {
-      case 10: run_g3<double, 10>(adj, it, ni, grid, xs, perm, f, g, s); return;
-      case 14: run_g3<double, 14>(adj, it, ni, grid, xs, perm, f, g, s); return;
+      case 10: run_g3<double, 10>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
+      case 14: run_g3<double, 14>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
     }
     fatal("no 3-D group kernel for w=%d", g.w);
   }
@@ -80,35 +105,42 @@ bool group3_supported(int w) { return G3Set<R>::has(w); }
 template <typename R>
 size_t group3_smem_bytes(const Geom<R> &g) { return G3Set<R>::smem(g); }
 int group3_subcell_edge() { return G3_CS; }
+template <typename R>
+bool group3_column_supported(int w) { return G3Set<R>::column(w); }
 int group3_max_item() { return G3_MAXITEM; }
 
 template <typename R>
 void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
-                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
+                     cudaStream_t s)
 {
   if (nitems > 0)
-    G3Set<R>::run(false, items, nitems, const_cast<typename Cx<R>::T *>(grid), xs, perm, f, g, s);
+    G3Set<R>::run(false, items, nitems, const_cast<typename Cx<R>::T *>(grid), xs, perm, f, g, poly, s);
 }
 
 template <typename R>
 void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
-                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
+                      cudaStream_t s)
 {
   if (nitems > 0)
-    G3Set<R>::run(true, items, nitems, grid, xs, perm, const_cast<typename Cx<R>::T *>(f), g, s);
+    G3Set<R>::run(true, items, nitems, grid, xs, perm, const_cast<typename Cx<R>::T *>(f), g, poly, s);
 }
 
 template bool group3_supported<float>(int);
 template bool group3_supported<double>(int);
 template size_t group3_smem_bytes<float>(const Geom<float> &);
+template bool group3_column_supported<float>(int);
+template bool group3_column_supported<double>(int);
 template size_t group3_smem_bytes<double>(const Geom<double> &);
 template void launch_b3_group<float>(const WorkItem *, int, const float2 *, const float *, const uint32_t *,
-                                     float2 *, const Geom<float> &, cudaStream_t);
+                                     float2 *, const Geom<float> &, const WinPoly &, cudaStream_t);
 template void launch_b3_group<double>(const WorkItem *, int, const double2 *, const double *,
-                                      const uint32_t *, double2 *, const Geom<double> &, cudaStream_t);
+                                      const uint32_t *, double2 *, const Geom<double> &, const WinPoly &,
+                                      cudaStream_t);
 template void launch_bt3_group<float>(const WorkItem *, int, float2 *, const float *, const uint32_t *,
-                                      const float2 *, const Geom<float> &, cudaStream_t);
+                                      const float2 *, const Geom<float> &, const WinPoly &, cudaStream_t);
 template void launch_bt3_group<double>(const WorkItem *, int, double2 *, const double *, const uint32_t *,
-                                       const double2 *, const Geom<double> &, cudaStream_t);
+                                       const double2 *, const Geom<double> &, const WinPoly &, cudaStream_t);
 
 }  // namespace gb

@@ -1,0 +1,568 @@
+// gb_col3.cuh -- single-precision 3-D B^T (adjoint spreading) by z-columns
+// and 3-D B (interpolation) by sub-cell units: the hot kernels of the 3-D
+// transform.
+//
+// Both evaluate the Kaiser-Bessel window on the fly from its per-tap
+// polynomial form (gb_window.cpp): degree-9 Horner in the node's fractional
+// grid offset, single-precision FMAs with the coefficients as kernel
+// parameters.
+//
+// B^T -- reference nfft_adjoint_3d_B (nfft.c:5126-5384) with its blockwise
+// scatter (nfft.c:4289-4388): g[l mod n] += phi_0 phi_1 phi_2 f_j over the
+// (2m+2)^3 window of every node.
+//
+// Node set-up sorts the nodes by (8^3 tile, 2x2 column of the tile's x/y
+// cells, window start along z), so the nodes of one column sit together,
+// ordered by their z window start z0 in [0, 8).  A column's nodes all touch
+// the same W+1 by W+1 (x, y) rows of the tile's padded subgrid, over z in
+// [0, 8 + W - 1).
+//
+// A CTA takes one work item (a tile and a range of its nodes) and keeps the
+// tile's padded subgrid in shared memory as interleaved complex values.  A
+// warp takes a column chunk (at most 32 nodes of one column):
+//  * lane j evaluates node j's window into per-warp vectors: x scaled by f_j
+//    (complex), y, and z duplicated as (w, w) pairs;
+//  * lanes own (x, y) rows of the column (two per lane) and hold all
+//    8 + W - 1 z values of a row as complex accumulators in registers; for the
+//    nodes whose window starts at z0 (a compile-time case, eight of them)
+//    each row takes exactly W paired FMAs (fma.rn.f32x2 of the sm_100
+//    family: real and imaginary at once);
+//  * each row is added to the shared subgrid once per chunk.  Single-precision
+//    atomic adds on shared memory are compare-and-swap loops, one value at a
+//    time; here a row's complex cells are read, summed and swapped as 64-bit
+//    words, all of them before the first result is checked, and only the
+//    rare cell another warp changed in between is added again;
+//  * the subgrid goes to the global grid once per work item with vector
+//    reductions.
+#pragma once
+
+#include "gb_b3group.cuh"  // warp_transpose_reduce
+#include "gb_internal.h"
+
+namespace gb {
+
+static constexpr int C3_THREADS = 256;
+static constexpr int C3_WARPS = C3_THREADS / 32;
+static constexpr int C3_CHUNK = 32;  // nodes per column chunk (one per lane at set-up)
+
+template <int W>
+struct C3 {
+  static constexpr int EXT = 8 + W - 1;                      // padded subgrid edge
+  static constexpr int BOX = W + 1;                          // rows per dimension of a column
+  static constexpr int BOXP = (BOX + 3) / 4 * 4;             // padded x / y vector length
+  static constexpr int ROWS = BOX * BOX;                     // (x, y) rows of a column
+  static constexpr int RPL = 2;                              // rows a lane holds at once
+  static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
+  // per-warp scratch (floats): x scaled by f [CHUNK][BOXP] complex, y
+  // [CHUNK][BOXP], z duplicated [CHUNK][W] pairs
+  static constexpr int WXF = 0;
+  static constexpr int WY = WXF + 2 * BOXP * C3_CHUNK;
+  static constexpr int WZ = WY + BOXP * C3_CHUNK;
+  static constexpr int WARP_FLOATS = WZ + 2 * W * C3_CHUNK;
+  static constexpr int INTS = 17 + 1;                        // column starts, task counter
+  static_assert(BOXP > BOX, "x / y vectors need one zero slot past the column");
+  static_assert((2 * W) % 4 == 0, "z pair vectors are read four floats at a time");
+};
+
+template <int W>
+inline size_t c3_smem_bytes(const Geom<float> &g)
+{
+  typedef C3<W> P;
+  return (size_t)C3_WARPS * P::WARP_FLOATS * sizeof(float) + (size_t)P::EXT * g.sx2 * sizeof(float2)
+         + P::INTS * sizeof(int);
+}
+
+// window start (unwrapped index - tile origin) of a node in dimension t;
+// t0 = n x - u in [m, m + 1)
+__device__ __forceinline__ int c3_loc(float x, int t, const Geom<float> &g, int org_t, float &t0)
+{
+  const float xn = x * g.nR[t];
+  const int u = (int)floorf(xn) - g.m;
+  t0 = xn - (float)u;
+  return wrap(u, g.n[t]) - org_t;
+}
+
+__device__ __forceinline__ unsigned long long f2_bits(float2 v)
+{
+  return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
+}
+__device__ __forceinline__ float2 bits_f2(unsigned long long b)
+{
+  return make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32)));
+}
+
+// Adds v[z] to the interleaved complex cells p[z] for z in [z1, z2) (a
+// warp-uniform range), ZB cells at a time: every cell of a block is read,
+// summed and offered by one 64-bit compare-and-swap before any result is
+// checked; a cell whose swap found a value changed by another warp in
+// between is added again with the atomic add of each component.
+template <int N, int ZB>
+__device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&v)[N], int z1, int z2)
+{
+#pragma unroll
+  for (int z0 = 0; z0 < N; z0 += ZB) {
+    unsigned long long cur[ZB];
+#pragma unroll
+    for (int e = 0; e < ZB; ++e) {
+      const int z = z0 + e;
+      if (z < N && z >= z1 && z < z2) cur[e] = *reinterpret_cast<volatile unsigned long long *>(p + z);
+    }
+    unsigned miss = 0;
+#pragma unroll
+    for (int e = 0; e < ZB; ++e) {
+      const int z = z0 + e;
+      if (z < N && z >= z1 && z < z2) {
+        const float2 o = bits_f2(cur[e]);
+        const unsigned long long want = f2_bits(make_float2(o.x + v[z].x, o.y + v[z].y));
+        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z), cur[e], want) != cur[e]) miss |= 1u << e;
+      }
+    }
+    if (miss) {
+#pragma unroll
+      for (int e = 0; e < ZB; ++e) {
+        const int z = z0 + e;
+        if (z < N && (miss >> e) & 1u) {
+          atomicAdd(&p[z].x, v[z].x);
+          atomicAdd(&p[z].y, v[z].y);
+        }
+      }
+    }
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__restrict__ items,
+                                                            float2 *__restrict__ grid,
+                                                            const float *__restrict__ xs,
+                                                            const uint32_t *__restrict__ perm,
+                                                            const float2 *__restrict__ f, Geom<float> g,
+                                                            WinPoly poly)
+{
+  typedef C3<W> P;
+  constexpr int EXT = P::EXT, BOXP = P::BOXP, RPL = P::RPL;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *const base = reinterpret_cast<float *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *const wsc = base + warp * P::WARP_FLOATS;
+  float2 *const wxf = reinterpret_cast<float2 *>(wsc + P::WXF);
+  float *const wy = wsc + P::WY;
+  float2 *const wz2 = reinterpret_cast<float2 *>(wsc + P::WZ);
+  float2 *const sg = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
+  int *const cstart = reinterpret_cast<int *>(sg + EXT * g.sx2);
+  int *const taskctr = cstart + 17;
+
+  const WorkItem it = items[blockIdx.x];
+  int org[3];
+  {
+    int rem = it.tile;
+#pragma unroll
+    for (int t = 2; t >= 0; --t) {
+      org[t] = (rem % g.ntile[t]) * 8;
+      rem /= g.ntile[t];
+    }
+  }
+  for (int i = threadIdx.x; i < EXT * g.sx2; i += C3_THREADS) sg[i] = make_float2(0.f, 0.f);
+  // column boundaries of the item: cstart[c] = first node whose column >= c
+  const int n = it.end - it.start;
+  for (int k = threadIdx.x; k <= n; k += C3_THREADS) {
+    float t0;
+    int ck = 16, cp = -1;
+    if (k < n) {
+      const float *x3 = xs + 3LL * (it.start + k);
+      ck = (c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1);
+    }
+    if (k > 0) {
+      const float *x3 = xs + 3LL * (it.start + k - 1);
+      cp = (c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1);
+    }
+    for (int c = cp + 1; c <= ck; ++c) cstart[c] = k;
+  }
+  if (threadIdx.x == 0) *taskctr = 0;
+  __syncthreads();
+
+  // chunks per column (lanes 0..15), inclusive scan -> task -> column map
+  int nch = 0;
+  if (lane < 16) nch = (cstart[lane + 1] - cstart[lane] + C3_CHUNK - 1) / C3_CHUNK;
+  int incl = nch;
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int ntask = __shfl_sync(0xffffffffu, incl, 15);
+
+  for (;;) {
+    int task = 0;
+    if (lane == 0) task = atomicAdd(taskctr, 1);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= ntask) break;
+    // column c = number of columns whose inclusive chunk count is <= task
+    const int c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
+    const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);  // lane c - 1 (c is warp-uniform)
+    const int before = c > 0 ? prev : 0;
+    const int clen = cstart[c + 1] - cstart[c];
+    const int nchunk = (clen + C3_CHUNK - 1) / C3_CHUNK;
+    // the column's nodes split evenly into its chunks
+    const int k = task - before, qn = clen / nchunk, rq = clen - qn * nchunk;
+    const int a = it.start + cstart[c] + k * qn + min(k, rq);
+    const int np = qn + (k < rq ? 1 : 0);
+    const int s0 = c >> 2, s1 = c & 3;
+
+    // ---- set-up: lane j evaluates node j's window
+    int z0 = 8;
+    if (lane < np) {
+      const int i = a + lane;
+      const float *x3 = xs + 3LL * i;
+      const float2 fj = f[perm[i]];
+      float t0;
+      float v[W];
+      // x, scaled by f_j, at the node's offset in the column's box
+      const int ox = c3_loc(x3[0], 0, g, org[0], t0) - 2 * s0;
+      kb_poly_taps<W>(t0, g.m, poly.c[0], v);
+      {
+        float4 *dst = reinterpret_cast<float4 *>(wxf + lane * BOXP);
+#pragma unroll
+        for (int q = 0; q < BOXP / 2; ++q) {
+          float e[4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int b = 2 * q + h;
+            float val = 0.f;
+            if (b < W && ox == 0) val = v[b];
+            if (b >= 1 && b - 1 < W && ox == 1) val = v[b - 1];
+            e[2 * h] = val * fj.x;
+            e[2 * h + 1] = val * fj.y;
+          }
+          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+        }
+      }
+      const int oy = c3_loc(x3[1], 1, g, org[1], t0) - 2 * s1;
+      kb_poly_taps<W>(t0, g.m, poly.c[1], v);
+      {
+        float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
+#pragma unroll
+        for (int q = 0; q < BOXP / 4; ++q) {
+          float e[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int b = 4 * q + h;
+            float val = 0.f;
+            if (b < W && oy == 0) val = v[b];
+            if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
+            e[h] = val;
+          }
+          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+        }
+      }
+      z0 = c3_loc(x3[2], 2, g, org[2], t0);
+      kb_poly_taps<W>(t0, g.m, poly.c[2], v);
+      {
+        float4 *dst = reinterpret_cast<float4 *>(wz2 + lane * W);
+#pragma unroll
+        for (int q = 0; q < W / 2; ++q) dst[q] = make_float4(v[2 * q], v[2 * q], v[2 * q + 1], v[2 * q + 1]);
+      }
+    }
+    // runs of equal z0 (the chunk is sorted by z0): rs[z] = first lane with z0 >= z
+    int rs[9];
+#pragma unroll
+    for (int z = 0; z <= 8; ++z) rs[z] = __popc(__ballot_sync(0xffffffffu, z0 < z));
+    __syncwarp();
+    int zmin = 8, zmax = -1;
+#pragma unroll
+    for (int z = 0; z < 8; ++z)
+      if (rs[z + 1] > rs[z]) {
+        zmin = min(zmin, z);
+        zmax = z;
+      }
+
+#pragma unroll 1
+    for (int ri = 0; ri < P::RITER; ++ri) {
+      int bx[RPL], by[RPL];
+      bool ok[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        const int row = lane + 32 * (ri * RPL + q);
+        ok[q] = row < P::ROWS;
+        // rows past the column read the zero slot BOXP - 1 of the x vector
+        bx[q] = ok[q] ? row / P::BOX : BOXP - 1;
+        by[q] = ok[q] ? row - (row / P::BOX) * P::BOX : 0;
+      }
+      float2 acc[RPL][EXT];
+#pragma unroll
+      for (int q = 0; q < RPL; ++q)
+#pragma unroll
+        for (int z = 0; z < EXT; ++z) acc[q][z] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int zz = 0; zz < 8; ++zz) {
+#pragma unroll 1
+        for (int j = rs[zz]; j < rs[zz + 1]; ++j) {
+          float2 w[W];
+          const float4 *src = reinterpret_cast<const float4 *>(wz2 + j * W);
+#pragma unroll
+          for (int q = 0; q < W / 2; ++q) {
+            const float4 t = src[q];
+            w[2 * q] = make_float2(t.x, t.y);
+            w[2 * q + 1] = make_float2(t.z, t.w);
+          }
+#pragma unroll
+          for (int q = 0; q < RPL; ++q) {
+            const float2 xf = wxf[j * BOXP + bx[q]];
+            const float yv = wy[j * BOXP + by[q]];
+            const float2 h = make_float2(xf.x * yv, xf.y * yv);
+#pragma unroll
+            for (int z = 0; z < W; ++z) acc[q][zz + z] = __ffma2_rn(w[z], h, acc[q][zz + z]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPL; ++q)
+        if (ok[q]) c3_flush_row<EXT, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, acc[q], zmin, zmax + W);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // one vector reduction per non-zero cell of the padded subgrid
+  for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
+    const int c2 = idx % EXT, r = idx / EXT;
+    const int c1 = r % EXT, c0 = r / EXT;
+    const float2 v = sg[c0 * g.sx2 + c1 * g.sy2 + c2];
+    if (v.x == 0.f && v.y == 0.f) continue;
+    int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
+    while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+    while (p1 >= g.n[1]) p1 -= g.n[1];
+    while (p2 >= g.n[2]) p2 -= g.n[2];
+    global_add_c(grid + ((long long)p0 * g.n[1] + p1) * g.n[2] + p2, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// B -- 3-D interpolation by sub-cell units: f_j = sum phi_0 phi_1 phi_2 g over
+// the window of every node (reference nfft_trafo_3d_B, nfft.c:4687-4914, with
+// nfft_trafo_3d_compute, nfft.c:4020-4265).
+//
+// The nodes of a 2x2x2 sub-cell of a tile share one (W+1)^3 box of the padded
+// subgrid.  A CTA stages its tile's padded subgrid in shared memory (real and
+// imaginary planes), finds where each of the tile's 64 sub-cells starts in the
+// item's sorted node range, and its warps take units (at most S3_PM nodes of
+// one sub-cell, a sub-cell's nodes split evenly) from a shared counter:
+//  * lanes evaluate the unit's windows (one lane per node and dimension) into
+//    zero-padded per-warp vectors at each node's offset in the box;
+//  * lanes own two (x, y) box rows at a time and hold their W+1 z values in
+//    registers; nodes go in pairs, so the paired z FMAs (fma.rn.f32x2) of two
+//    nodes and two rows are independent chains;
+//  * the per-lane partial sums of the unit's nodes meet in one butterfly
+//    transpose-reduction.
+static constexpr int S3_PM = 16;  // nodes per unit
+
+template <int W>
+struct S3 {
+  static constexpr int EXT = 8 + W - 1;
+  static constexpr int BOX = W + 1;
+  static constexpr int BOXP = (BOX + 3) / 4 * 4;
+  static constexpr int ROWS = BOX * BOX;
+  static constexpr int RPL = 2;
+  static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
+  static constexpr int WARP_FLOATS = 3 * S3_PM * BOXP;  // wx, wy, wz [S3_PM][BOXP]
+  static constexpr int INTS = 65 + 1;                   // sub-cell starts, task counter
+  static_assert(BOXP > BOX, "the x vector needs one zero slot past the box");
+};
+
+template <int W>
+inline size_t s3_smem_bytes(const Geom<float> &g)
+{
+  typedef S3<W> P;
+  return ((size_t)C3_WARPS * P::WARP_FLOATS + 2 * (size_t)P::EXT * g.sx) * sizeof(float)
+         + P::INTS * sizeof(int);
+}
+
+// sub-cell (2x2x2) of a node inside its tile, row-major over the tile's 4^3
+__device__ __forceinline__ int s3_subcell(const float *x3, const Geom<float> &g, const int *org)
+{
+  float t0;
+  return ((c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1)) * 4
+         + (c3_loc(x3[2], 2, g, org[2], t0) >> 1);
+}
+
+template <int W>
+__global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__restrict__ items,
+                                                            const float2 *__restrict__ grid,
+                                                            const float *__restrict__ xs,
+                                                            const uint32_t *__restrict__ perm,
+                                                            float2 *__restrict__ f, Geom<float> g,
+                                                            WinPoly poly)
+{
+  typedef S3<W> P;
+  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RPL = P::RPL, PM = S3_PM;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *const base = reinterpret_cast<float *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *const wx = base + warp * P::WARP_FLOATS;
+  float *const wy = wx + PM * BOXP;
+  float *const wz = wy + PM * BOXP;
+  float *const sre = base + C3_WARPS * P::WARP_FLOATS;
+  float *const sim = sre + EXT * g.sx;
+  int *const sstart = reinterpret_cast<int *>(sim + EXT * g.sx);
+  int *const taskctr = sstart + 65;
+
+  const WorkItem it = items[blockIdx.x];
+  int org[3];
+  {
+    int rem = it.tile;
+#pragma unroll
+    for (int t = 2; t >= 0; --t) {
+      org[t] = (rem % g.ntile[t]) * 8;
+      rem /= g.ntile[t];
+    }
+  }
+  // stage the padded subgrid; several grid loads in flight per thread
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
+    const int c2 = idx % EXT, r = idx / EXT;
+    const int c1 = r % EXT, c0 = r / EXT;
+    int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
+    while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+    while (p1 >= g.n[1]) p1 -= g.n[1];
+    while (p2 >= g.n[2]) p2 -= g.n[2];
+    const float2 v = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
+    const int si = c0 * g.sx + c1 * g.sy + c2;
+    sre[si] = v.x;
+    sim[si] = v.y;
+  }
+  // the unused node slots of the weight vectors must hold finite values
+  for (int i = lane; i < P::WARP_FLOATS; i += 32) wx[i] = 0.f;
+  // sub-cell boundaries: sstart[s] = first node of the item whose sub-cell >= s
+  const int n = it.end - it.start;
+  for (int k = threadIdx.x; k <= n; k += C3_THREADS) {
+    const int ck = k < n ? s3_subcell(xs + 3LL * (it.start + k), g, org) : 64;
+    const int cp = k > 0 ? s3_subcell(xs + 3LL * (it.start + k - 1), g, org) : -1;
+    for (int c = cp + 1; c <= ck; ++c) sstart[c] = k;
+  }
+  if (threadIdx.x == 0) *taskctr = 0;
+  __syncthreads();
+
+  // units per sub-cell: lane l holds sub-cells 2l and 2l+1
+  const int l0 = sstart[2 * lane + 1] - sstart[2 * lane], l1 = sstart[2 * lane + 2] - sstart[2 * lane + 1];
+  const int n0 = (l0 + PM - 1) / PM, n1 = (l1 + PM - 1) / PM;
+  int incl = n0 + n1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int ntask = __shfl_sync(0xffffffffu, incl, 31);
+
+  for (;;) {
+    int task = 0;
+    if (lane == 0) task = atomicAdd(taskctr, 1);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= ntask) break;
+    const int L = __popc(__ballot_sync(0xffffffffu, incl <= task));  // lane holding the task
+    const int excl = incl - n0 - n1;
+    const bool second = task - excl >= n0;
+    const int s_l = 2 * lane + (second ? 1 : 0);
+    const int k_l = task - excl - (second ? n0 : 0);
+    const int nu_l = second ? n1 : n0;
+    const int len_l = second ? l1 : l0;
+    const int s = __shfl_sync(0xffffffffu, s_l, L);
+    const int k = __shfl_sync(0xffffffffu, k_l, L);
+    const int nu = __shfl_sync(0xffffffffu, nu_l, L);
+    const int len = __shfl_sync(0xffffffffu, len_l, L);
+    // the sub-cell's nodes split evenly into nu units
+    const int q = len / nu, rq = len - q * nu;
+    const int u0 = it.start + sstart[s] + k * q + min(k, rq);
+    const int np = q + (k < rq ? 1 : 0);
+    const int b0 = (s >> 4) * 2, b1 = ((s >> 2) & 3) * 2, b2 = (s & 3) * 2;
+
+    // ---- windows: lane k < 3 np takes node k / 3, dimension k mod 3
+    for (int kk = lane; kk < 3 * np; kk += 32) {
+      const int j = kk / 3, t = kk - 3 * j;
+      float t0;
+      const int loc = c3_loc(xs[3LL * (u0 + j) + t], t, g, t == 0 ? org[0] : (t == 1 ? org[1] : org[2]), t0);
+      const int o = loc - (t == 0 ? b0 : (t == 1 ? b1 : b2));
+      float v[W];
+      if (poly.same) kb_poly_taps<W>(t0, g.m, poly.c[0], v);
+      else kb_poly_taps<W>(t0, g.m, poly.c[t], v);
+      float *dst = wx + (t * PM + j) * BOXP;
+      float e[BOXP];
+#pragma unroll
+      for (int b = 0; b < BOXP; ++b) {
+        float val = 0.f;
+        if (b < W && o == 0) val = v[b];
+        if (b >= 1 && b - 1 < W && o == 1) val = v[b - 1];
+        e[b] = val;
+      }
+#pragma unroll
+      for (int b = 0; b < BOXP; b += 4) *reinterpret_cast<float4 *>(dst + b) = make_float4(e[b], e[b + 1], e[b + 2], e[b + 3]);
+    }
+    __syncwarp();
+
+    const int sbase = b0 * g.sx + b1 * g.sy + b2;
+    float acc[2 * PM];
+#pragma unroll
+    for (int j = 0; j < 2 * PM; ++j) acc[j] = 0.f;
+#pragma unroll 1
+    for (int ri = 0; ri < P::RITER; ++ri) {
+      int wbx[RPL], by[RPL];
+      float gr[RPL][BOX], gi[RPL][BOX];
+#pragma unroll
+      for (int qq = 0; qq < RPL; ++qq) {
+        const int row = lane + 32 * (ri * RPL + qq);
+        const bool ok = row < P::ROWS;
+        const int rr = ok ? row : 0;
+        const int bx = rr / BOX;
+        by[qq] = rr - bx * BOX;
+        wbx[qq] = ok ? bx : BOXP - 1;  // rows past the box take the zero slot of the x vector
+        const float *pr = sre + sbase + bx * g.sx + by[qq] * g.sy;
+        const float *pi = sim + sbase + bx * g.sx + by[qq] * g.sy;
+#pragma unroll
+        for (int z = 0; z < BOX; ++z) {
+          gr[qq][z] = pr[z];
+          gi[qq][z] = pi[z];
+        }
+      }
+#pragma unroll
+      for (int jb = 0; jb < PM; jb += 2) {
+        if (jb < np) {
+#pragma unroll
+          for (int j = jb; j < jb + 2; ++j) {
+            float wzj[BOXP];
+#pragma unroll
+            for (int b = 0; b < BOXP; b += 4) {
+              const float4 t = *reinterpret_cast<const float4 *>(wz + j * BOXP + b);
+              wzj[b] = t.x;
+              wzj[b + 1] = t.y;
+              wzj[b + 2] = t.z;
+              wzj[b + 3] = t.w;
+            }
+#pragma unroll
+            for (int qq = 0; qq < RPL; ++qq) {
+              float2 r2 = make_float2(0.f, 0.f), i2 = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int z = 0; z + 1 < BOX; z += 2) {
+                const float2 w2 = make_float2(wzj[z], wzj[z + 1]);
+                r2 = __ffma2_rn(w2, make_float2(gr[qq][z], gr[qq][z + 1]), r2);
+                i2 = __ffma2_rn(w2, make_float2(gi[qq][z], gi[qq][z + 1]), i2);
+              }
+              float tr = r2.x + r2.y, ti = i2.x + i2.y;
+              if (BOX & 1) {
+                tr = fmaf(wzj[BOX - 1], gr[qq][BOX - 1], tr);
+                ti = fmaf(wzj[BOX - 1], gi[qq][BOX - 1], ti);
+              }
+              const float wxy = wx[j * BOXP + wbx[qq]] * wy[j * BOXP + by[qq]];
+              acc[2 * j] = fmaf(wxy, tr, acc[2 * j]);
+              acc[2 * j + 1] = fmaf(wxy, ti, acc[2 * j + 1]);
+            }
+          }
+        }
+      }
+    }
+    if (np > 8) warp_transpose_reduce<float, 32>(acc);
+    else warp_transpose_reduce<float, 16>(acc);
+    const float re = __shfl_sync(0xffffffffu, acc[0], (2 * lane) & 31);
+    const float im = __shfl_sync(0xffffffffu, acc[0], (2 * lane + 1) & 31);
+    if (lane < np) f[perm[u0 + lane]] = make_float2(re, im);
+    __syncwarp();
+  }
+}
+
+}  // namespace gb

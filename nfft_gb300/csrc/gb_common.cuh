@@ -51,9 +51,23 @@ struct Geom {
   int ntile[GB_MAXD];    // tiles per dim (n_t / T_t, rounded up)
   int ext[GB_MAXD];      // padded subgrid edge T_t + w - 1
   int cs;                // sub-cell edge of the 3-D group kernels (1 = off)
-  int sub;               // sub-cells per tile ((T/cs)^d, 1 = off)
+  int csz;               // sub-cell edge along the last dimension (z-column kernels: 1)
+  int sub;               // sub-cells per tile ((T/cs)^(d-1) (T/csz), 1 = off)
   int sx, sy;            // shared-memory plane strides of the group kernels (x, y)
+  int sx2, sy2;          // the same for subgrids of interleaved complex values
 };
+
+// Polynomial form of the Kaiser-Bessel window (single-precision 3-D
+// kernels): tap l of a node is sum_k c[t][l][k] s^k with s = 2 frac(n x) - 1.
+#define KB_POLY_DP 10    // coefficients per tap (degree 9)
+#define KB_POLY_WMAX 10  // widest window with a polynomial form
+struct WinPoly {
+  float c[3][KB_POLY_WMAX][KB_POLY_DP];  // per dimension, tap, increasing power of s
+  int same;                              // every dimension has the same b (c[0] serves all)
+};
+// fills coef[l * KB_POLY_DP + k] for the w taps of the window with cut-off m
+// and shape b (host, double precision)
+void kb_poly_fit(int m, double b, int w, float *coef);
 
 struct WorkItem {
   int tile;    // linear tile id (row-major over ntile)
@@ -135,6 +149,22 @@ __device__ __forceinline__ float kb_phi_t_fast(float t, float mm, float b)
 }
 
 __device__ __forceinline__ float kb_window_t(float t, float mm, float b) { return kb_phi_t_fast(t, mm, b); }
+
+// the W taps of a node from its polynomial form: t0 = n x - u in [m, m+1)
+template <int W>
+__device__ __forceinline__ void kb_poly_taps(float t0, int m, const float (&c)[KB_POLY_WMAX][KB_POLY_DP],
+                                             float (&v)[W])
+{
+  static_assert(W <= KB_POLY_WMAX, "no polynomial form for this width");
+  const float s = fmaf(2.f, t0, -(float)(2 * m + 1));  // exact: 2 (t0 - m) - 1
+#pragma unroll
+  for (int l = 0; l < W; ++l) {
+    float a = c[l][KB_POLY_DP - 1];
+#pragma unroll
+    for (int k = KB_POLY_DP - 2; k >= 0; --k) a = fmaf(a, s, c[l][k]);
+    v[l] = a;
+  }
+}
 __device__ __forceinline__ double kb_window_t(double t, double mm, double b) { return kb_phi_t<double>(t, mm, b); }
 
 // Unwrapped window start u = floor(x n) - m (reference nfft.c:324-332).  The

@@ -71,13 +71,18 @@ bool group3_supported(int w);
 template <typename R>
 size_t group3_smem_bytes(const Geom<R> &g);
 int group3_subcell_edge();
+// z-column B^T kernel (nodes keyed by (x sub-cell, y sub-cell, z cell))
+template <typename R>
+bool group3_column_supported(int w);
 int group3_max_item();
 template <typename R>
 void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
-                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
+                     const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
+                     cudaStream_t s);
 template <typename R>
 void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
-                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s);
+                      const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
+                      cudaStream_t s);
 // generic global-memory kernels for any d and m
 template <typename R>
 void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,

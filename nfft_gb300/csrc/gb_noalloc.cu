@@ -80,6 +80,7 @@ int sort_noalloc(const R *x_dev, int d, const int *n, int m, int M, long long *i
     if (t < d) g.n_total *= nt;
   }
   g.cs = 1;
+  g.csz = 1;
   g.sub = 1;
   if (g.n_total > 0xffffffffLL) {
     gb::record_error("nfft_gb_sort_nodes_noalloc: n_0 * ... * n_{d-1} must be below 2^32");

@@ -69,6 +69,7 @@ struct Ctx {
   bool direct = false;   // reference switches to the NDFT (nfft.c:5658-5665)
   bool tiled = false;
   bool group3 = false;  // 3-D sub-cell group kernels
+  WinPoly poly = {};     // polynomial window of the single-precision 3-D kernels
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // FFT: one plan for d <= 3; for d > 3 a rank-3 plan over the last three
@@ -151,17 +152,23 @@ static void choose_tiles(Ctx<R> *c)
   const int cs = group3_subcell_edge();
   c->group3 = false;
   g.cs = 1;
+  g.csz = 1;
   g.sub = 1;
   if (g.d == 3 && group3_supported<R>(g.w) && g.n[0] >= 8 && g.n[1] >= 8 && g.n[2] >= 8) {
     Geom<R> h = g;
     for (int t = 0; t < 3; ++t) h.ext[t] = 8 + g.w - 1;
     h.sx = h.ext[0] * (h.ext[0] + 8) + 40;  // upper bound of the padded plane stride
+    h.sx2 = h.ext[0] * (h.ext[0] + 16) + 40;
     if (group3_smem_bytes<R>(h) <= 200 * 1024) {
       c->group3 = true;
       c->tiled = true;
       T = 8;
       g.cs = cs;
-      g.sub = (8 / cs) * (8 / cs) * (8 / cs);
+      // the z-column B^T kernel wants its columns' nodes ordered by window
+      // start along z; the sub-cell B kernel only needs them grouped by
+      // sub-cell, which that finer order also gives
+      g.csz = group3_column_supported<R>(g.w) ? 1 : cs;
+      g.sub = (8 / cs) * (8 / cs) * (8 / g.csz);
       // plane strides: rows of a box taken 32 at a time by a warp should hit
       // distinct banks; search the padding that minimises the worst case
       const int ext = 8 + g.w - 1, box = g.w + cs - 1, rows = box * box;
@@ -184,6 +191,29 @@ static void choose_tiles(Ctx<R> *c)
             best = cost;
             g.sy = sy;
             g.sx = sx;
+          }
+        }
+      // interleaved complex (8-byte) rows: a warp's 64-bit accesses go out as
+      // two half-warps, whose 16 rows should fall on distinct bank pairs
+      best = 1 << 30;
+      g.sy2 = ext;
+      g.sx2 = ext * ext;
+      for (int sy = ext; sy < ext + 16; ++sy)
+        for (int sx = ext * sy; sx < ext * sy + 40; ++sx) {
+          int cost = 0;
+          for (int r0 = 0; r0 < rows; r0 += 16) {
+            int cnt[16] = {0}, worst = 0;
+            for (int l = 0; l < 16 && r0 + l < rows; ++l) {
+              const int r = r0 + l, bx = r / box, by = r % box;
+              worst = std::max(worst, ++cnt[(bx * sx + by * sy) & 15]);
+            }
+            cost += worst;
+          }
+          cost = cost * 4096 + (sx * ext);
+          if (cost < best) {
+            best = cost;
+            g.sy2 = sy;
+            g.sx2 = sx;
           }
         }
     }
@@ -337,6 +367,13 @@ static void init_help(typename Api<R>::plan *ths)
     g.n[t] = g.N[t] = 1;
     g.nR[t] = 1;
   }
+  if (g.w <= KB_POLY_WMAX) {
+    c->poly.same = 1;
+    for (int t = 0; t < std::min(d, 3); ++t) {
+      kb_poly_fit(g.m, (double)ths->b[t], g.w, &c->poly.c[t][0][0]);
+      if (ths->b[t] != ths->b[0]) c->poly.same = 0;
+    }
+  }
   c->flags = ths->flags;
   choose_tiles<R>(c);
 
@@ -486,7 +523,7 @@ static void ensure_nodes(typename Api<R>::plan *ths, Ctx<R> *c)
 template <typename R>
 static void b_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
-  if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
   else if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_b_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
@@ -506,7 +543,7 @@ static void bt_stage(Ctx<R> *c, const typename Cx<R>::T *f, cudaEvent_t *E)
 {
   GB_CUDA(cudaMemsetAsync(c->grid, 0, (size_t)c->g.n_total * sizeof(typename Cx<R>::T), c->stream));
   GB_CUDA(cudaEventRecord(E[6], c->stream));
-  if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
   else if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_bt_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }

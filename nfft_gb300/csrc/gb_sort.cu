@@ -245,7 +245,8 @@ __global__ void k_node_keys(const R *__restrict__ x, Geom<R> g, uint32_t *__rest
     const int tile = u / g.T[t];
     tk = tk * (uint32_t)g.ntile[t] + (uint32_t)tile;
     // sub-cell of the window start inside its tile (group kernels)
-    sk = sk * (uint32_t)(g.T[t] / g.cs) + (uint32_t)((u - tile * g.T[t]) / g.cs);
+    const int cst = (t == g.d - 1) ? g.csz : g.cs;
+    sk = sk * (uint32_t)(g.T[t] / cst) + (uint32_t)((u - tile * g.T[t]) / cst);
     // reference sort key: floor(n*x - m) in plan precision, no contraction
     const int help = (int)gb_floor(sub_rn(mul_rn(g.nR[t], xt), (R)g.m));
     const int ut = ((help % g.n[t]) + g.n[t]) % g.n[t];

@@ -13,7 +13,7 @@ static constexpr int G3_CS = 2;  // sub-cell edge
 template <typename R, int W>
 static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<R>::T *grid,
                    const R *xs, const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g,
-                   const WinPoly &poly, cudaStream_t s)
+                   const WinPoly &poly, const Col3Bufs &cb, cudaStream_t s)
 {
   (void)poly;
   if constexpr (std::is_same<R, float>::value && W == 10) {
@@ -23,7 +23,8 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
         GB_CUDA(cudaFuncSetAttribute(k_bt3_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr_col = true;
       }
-      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, xs, perm, f, g, poly);
+      launch_gather_c(f, perm, g.M, cb.fs, s);
+      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, cb.fs, g, poly);
       GB_LAUNCHED("bt3_col");
       return;
     }
@@ -32,7 +33,7 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
       GB_CUDA(cudaFuncSetAttribute(k_b3_cell<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
       attr_cell = true;
     }
-    k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, xs, perm, f, g, poly);
+    k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.sst, perm, f, g, poly);
     GB_LAUNCHED("b3_cell");
     return;
   }
@@ -68,12 +69,12 @@ template <> struct G3Set<float> {
   }
   static bool column(int w) { return w == 10; }
   static void run(bool adj, const WorkItem *it, int ni, float2 *grid, const float *xs, const uint32_t *perm,
-                  float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+                  float2 *f, const Geom<float> &g, const WinPoly &poly, const Col3Bufs &cb, cudaStream_t s)
   {
     switch (g.w) {
-      case 8: run_g3<float, 8>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
-      case 10: run_g3<float, 10>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
-      case 14: run_g3<float, 14>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
+      case 8: run_g3<float, 8>(adj, it, ni, grid, xs, perm, f, g, poly, cb, s); return;
+      case 10: run_g3<float, 10>(adj, it, ni, grid, xs, perm, f, g, poly, cb, s); return;
+      case 14: run_g3<float, 14>(adj, it, ni, grid, xs, perm, f, g, poly, cb, s); return;
     }
     fatal("no 3-D group kernel for w=%d", g.w);
   }
@@ -90,11 +91,11 @@ template <> struct G3Set<double> {
     return 0;
   }
   static void run(bool adj, const WorkItem *it, int ni, double2 *grid, const double *xs,
-                  const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPoly &poly, cudaStream_t s)
+                  const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPoly &poly, const Col3Bufs &cb, cudaStream_t s)
   {
     switch (g.w) {
-      case 10: run_g3<double, 10>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
-      case 14: run_g3<double, 14>(adj, it, ni, grid, xs, perm, f, g, poly, s); return;
+      case 10: run_g3<double, 10>(adj, it, ni, grid, xs, perm, f, g, poly, cb, s); return;
+      case 14: run_g3<double, 14>(adj, it, ni, grid, xs, perm, f, g, poly, cb, s); return;
     }
     fatal("no 3-D group kernel for w=%d", g.w);
   }
@@ -112,19 +113,19 @@ int group3_max_item() { return G3_MAXITEM; }
 template <typename R>
 void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
                      const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
-                     cudaStream_t s)
+                     const Col3Bufs &cb, cudaStream_t s)
 {
   if (nitems > 0)
-    G3Set<R>::run(false, items, nitems, const_cast<typename Cx<R>::T *>(grid), xs, perm, f, g, poly, s);
+    G3Set<R>::run(false, items, nitems, const_cast<typename Cx<R>::T *>(grid), xs, perm, f, g, poly, cb, s);
 }
 
 template <typename R>
 void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
                       const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
-                      cudaStream_t s)
+                      const Col3Bufs &cb, cudaStream_t s)
 {
   if (nitems > 0)
-    G3Set<R>::run(true, items, nitems, grid, xs, perm, const_cast<typename Cx<R>::T *>(f), g, poly, s);
+    G3Set<R>::run(true, items, nitems, grid, xs, perm, const_cast<typename Cx<R>::T *>(f), g, poly, cb, s);
 }
 
 template bool group3_supported<float>(int);
@@ -134,13 +135,13 @@ template bool group3_column_supported<float>(int);
 template bool group3_column_supported<double>(int);
 template size_t group3_smem_bytes<double>(const Geom<double> &);
 template void launch_b3_group<float>(const WorkItem *, int, const float2 *, const float *, const uint32_t *,
-                                     float2 *, const Geom<float> &, const WinPoly &, cudaStream_t);
+                                     float2 *, const Geom<float> &, const WinPoly &, const Col3Bufs &, cudaStream_t);
 template void launch_b3_group<double>(const WorkItem *, int, const double2 *, const double *,
                                       const uint32_t *, double2 *, const Geom<double> &, const WinPoly &,
-                                      cudaStream_t);
+                                      const Col3Bufs &, cudaStream_t);
 template void launch_bt3_group<float>(const WorkItem *, int, float2 *, const float *, const uint32_t *,
-                                      const float2 *, const Geom<float> &, const WinPoly &, cudaStream_t);
+                                      const float2 *, const Geom<float> &, const WinPoly &, const Col3Bufs &, cudaStream_t);
 template void launch_bt3_group<double>(const WorkItem *, int, double2 *, const double *, const uint32_t *,
-                                       const double2 *, const Geom<double> &, const WinPoly &, cudaStream_t);
+                                       const double2 *, const Geom<double> &, const WinPoly &, const Col3Bufs &, cudaStream_t);
 
 }  // namespace gb

@@ -72,16 +72,6 @@ inline size_t c3_smem_bytes(const Geom<float> &g)
          + P::INTS * sizeof(int);
 }
 
-// window start (unwrapped index - tile origin) of a node in dimension t;
-// t0 = n x - u in [m, m + 1)
-__device__ __forceinline__ int c3_loc(float x, int t, const Geom<float> &g, int org_t, float &t0)
-{
-  const float xn = x * g.nR[t];
-  const int u = (int)floorf(xn) - g.m;
-  t0 = xn - (float)u;
-  return wrap(u, g.n[t]) - org_t;
-}
-
 __device__ __forceinline__ unsigned long long f2_bits(float2 v)
 {
   return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
@@ -133,9 +123,9 @@ __device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&v)[N], in
 template <int W>
 __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__restrict__ items,
                                                             float2 *__restrict__ grid,
-                                                            const float *__restrict__ xs,
-                                                            const uint32_t *__restrict__ perm,
-                                                            const float2 *__restrict__ f, Geom<float> g,
+                                                            const float4 *__restrict__ rec,
+                                                            const uint16_t *__restrict__ cst,
+                                                            const float2 *__restrict__ fs, Geom<float> g,
                                                             WinPoly poly)
 {
   typedef C3<W> P;
@@ -162,21 +152,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     }
   }
   for (int i = threadIdx.x; i < EXT * g.sx2; i += C3_THREADS) sg[i] = make_float2(0.f, 0.f);
-  // column boundaries of the item: cstart[c] = first node whose column >= c
-  const int n = it.end - it.start;
-  for (int k = threadIdx.x; k <= n; k += C3_THREADS) {
-    float t0;
-    int ck = 16, cp = -1;
-    if (k < n) {
-      const float *x3 = xs + 3LL * (it.start + k);
-      ck = (c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1);
-    }
-    if (k > 0) {
-      const float *x3 = xs + 3LL * (it.start + k - 1);
-      cp = (c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1);
-    }
-    for (int c = cp + 1; c <= ck; ++c) cstart[c] = k;
-  }
+  // column boundaries of the item (node set-up): cstart[c] = first node of column c
+  if (threadIdx.x < 17) cstart[threadIdx.x] = cst[17LL * blockIdx.x + threadIdx.x];
   if (threadIdx.x == 0) *taskctr = 0;
   __syncthreads();
 
@@ -211,14 +188,13 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     // ---- set-up: lane j evaluates node j's window
     int z0 = 8;
     if (lane < np) {
-      const int i = a + lane;
-      const float *x3 = xs + 3LL * i;
-      const float2 fj = f[perm[i]];
-      float t0;
+      const float4 r = rec[a + lane];
+      const float2 fj = fs[a + lane];
+      const int loc = __float_as_int(r.w);
       float v[W];
       // x, scaled by f_j, at the node's offset in the column's box
-      const int ox = c3_loc(x3[0], 0, g, org[0], t0) - 2 * s0;
-      kb_poly_taps<W>(t0, g.m, poly.c[0], v);
+      const int ox = (loc & 7) - 2 * s0;
+      kb_poly_taps_s<W>(r.x, poly.c[0], v);
       {
         float4 *dst = reinterpret_cast<float4 *>(wxf + lane * BOXP);
 #pragma unroll
@@ -236,8 +212,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
           dst[q] = make_float4(e[0], e[1], e[2], e[3]);
         }
       }
-      const int oy = c3_loc(x3[1], 1, g, org[1], t0) - 2 * s1;
-      kb_poly_taps<W>(t0, g.m, poly.c[1], v);
+      const int oy = ((loc >> 3) & 7) - 2 * s1;
+      kb_poly_taps_s<W>(r.y, poly.c[1], v);
       {
         float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
 #pragma unroll
@@ -254,8 +230,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
           dst[q] = make_float4(e[0], e[1], e[2], e[3]);
         }
       }
-      z0 = c3_loc(x3[2], 2, g, org[2], t0);
-      kb_poly_taps<W>(t0, g.m, poly.c[2], v);
+      z0 = loc >> 6;
+      kb_poly_taps_s<W>(r.z, poly.c[2], v);
       {
         float4 *dst = reinterpret_cast<float4 *>(wz2 + lane * W);
 #pragma unroll
@@ -375,18 +351,11 @@ inline size_t s3_smem_bytes(const Geom<float> &g)
          + P::INTS * sizeof(int);
 }
 
-// sub-cell (2x2x2) of a node inside its tile, row-major over the tile's 4^3
-__device__ __forceinline__ int s3_subcell(const float *x3, const Geom<float> &g, const int *org)
-{
-  float t0;
-  return ((c3_loc(x3[0], 0, g, org[0], t0) >> 1) * 4 + (c3_loc(x3[1], 1, g, org[1], t0) >> 1)) * 4
-         + (c3_loc(x3[2], 2, g, org[2], t0) >> 1);
-}
-
 template <int W>
 __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__restrict__ items,
                                                             const float2 *__restrict__ grid,
-                                                            const float *__restrict__ xs,
+                                                            const float4 *__restrict__ rec,
+                                                            const uint16_t *__restrict__ sst,
                                                             const uint32_t *__restrict__ perm,
                                                             float2 *__restrict__ f, Geom<float> g,
                                                             WinPoly poly)
@@ -430,13 +399,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
   }
   // the unused node slots of the weight vectors must hold finite values
   for (int i = lane; i < P::WARP_FLOATS; i += 32) wx[i] = 0.f;
-  // sub-cell boundaries: sstart[s] = first node of the item whose sub-cell >= s
-  const int n = it.end - it.start;
-  for (int k = threadIdx.x; k <= n; k += C3_THREADS) {
-    const int ck = k < n ? s3_subcell(xs + 3LL * (it.start + k), g, org) : 64;
-    const int cp = k > 0 ? s3_subcell(xs + 3LL * (it.start + k - 1), g, org) : -1;
-    for (int c = cp + 1; c <= ck; ++c) sstart[c] = k;
-  }
+  // sub-cell boundaries of the item (node set-up): sstart[s] = first node of sub-cell s
+  if (threadIdx.x < 65) sstart[threadIdx.x] = sst[65LL * blockIdx.x + threadIdx.x];
   if (threadIdx.x == 0) *taskctr = 0;
   __syncthreads();
 
@@ -476,12 +440,13 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
     // ---- windows: lane k < 3 np takes node k / 3, dimension k mod 3
     for (int kk = lane; kk < 3 * np; kk += 32) {
       const int j = kk / 3, t = kk - 3 * j;
-      float t0;
-      const int loc = c3_loc(xs[3LL * (u0 + j) + t], t, g, t == 0 ? org[0] : (t == 1 ? org[1] : org[2]), t0);
+      const float *rj = reinterpret_cast<const float *>(rec + u0 + j);
+      const float sj = rj[t];
+      const int loc = (__float_as_int(rj[3]) >> (3 * t)) & 7;
       const int o = loc - (t == 0 ? b0 : (t == 1 ? b1 : b2));
       float v[W];
-      if (poly.same) kb_poly_taps<W>(t0, g.m, poly.c[0], v);
-      else kb_poly_taps<W>(t0, g.m, poly.c[t], v);
+      if (poly.same) kb_poly_taps_s<W>(sj, poly.c[0], v);
+      else kb_poly_taps_s<W>(sj, poly.c[t], v);
       float *dst = wx + (t * PM + j) * BOXP;
       float e[BOXP];
 #pragma unroll

@@ -1,0 +1,77 @@
+// gb_col3_setup.cu -- node set-up for the single-precision 3-D kernels of
+// gb_col3.cuh, done once per node set (in precompute_one_psi), and the
+// per-call gather of the adjoint's input into tile order.
+//
+// The reference precomputes per-node window data once per node set as well
+// (PRE_PSI tables, nfft.c:5819-5844); here a node keeps 16 bytes: its three
+// polynomial arguments s_t = 2 frac(n_t x_t) - 1 and its window start inside
+// its 8^3 tile, three 3-bit fields.  Per work item the start of every z-column
+// (17 entries) and of every 2x2x2 sub-cell (65 entries) within the item's
+// node range is kept, so the transform kernels need no pass over the nodes to
+// find them.
+#include "gb_internal.h"
+
+namespace gb {
+
+__global__ void k_c3_records(const float *__restrict__ xs, Geom<float> g, float4 *__restrict__ rec)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.M) return;
+  float s[3];
+  int loc = 0;
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const float xn = xs[3 * i + t] * g.nR[t];
+    const int u = (int)floorf(xn) - g.m;  // node_u: the binning used the same expression
+    const float t0 = xn - (float)u;       // in [m, m + 1), exact
+    s[t] = fmaf(2.f, t0, -(float)(2 * g.m + 1));
+    loc |= (wrap(u, g.n[t]) & 7) << (3 * t);
+  }
+  rec[i] = make_float4(s[0], s[1], s[2], __int_as_float(loc));
+}
+
+// one block per work item; keys are the sorted node keys tile * sub + k with
+// k = (x sub-cell * 4 + y sub-cell) * 8 + z cell
+__global__ void k_c3_item_starts(const WorkItem *__restrict__ items, const uint32_t *__restrict__ keys,
+                                 uint32_t sub, uint16_t *__restrict__ cst, uint16_t *__restrict__ sst)
+{
+  const WorkItem it = items[blockIdx.x];
+  const int n = it.end - it.start;
+  uint16_t *c = cst + 17LL * blockIdx.x;
+  uint16_t *s = sst + 65LL * blockIdx.x;
+  for (int k = threadIdx.x; k <= n; k += blockDim.x) {
+    const int kc = k < n ? (int)(keys[it.start + k] % sub) : 128;
+    const int kp = k > 0 ? (int)(keys[it.start + k - 1] % sub) : -2;
+    for (int q = (kp >> 3) + 1; q <= (kc >> 3); ++q) c[q] = (uint16_t)k;
+    for (int q = (kp >> 1) + 1; q <= (kc >> 1); ++q) s[q] = (uint16_t)k;
+  }
+}
+
+__global__ void k_gather_c(const float2 *__restrict__ f, const uint32_t *__restrict__ perm, long long M,
+                           float2 *__restrict__ fs)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < M) fs[i] = f[perm[i]];
+}
+
+void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *items, int nitems,
+                     const uint32_t *keys, float4 *rec, uint16_t *cst, uint16_t *sst, cudaStream_t s)
+{
+  if (g.M > 0) {
+    k_c3_records<<<(unsigned)((g.M + 255) / 256), 256, 0, s>>>(xs, g, rec);
+    GB_LAUNCHED("c3_records");
+  }
+  if (nitems > 0) {
+    k_c3_item_starts<<<nitems, 128, 0, s>>>(items, keys, (uint32_t)g.sub, cst, sst);
+    GB_LAUNCHED("c3_item_starts");
+  }
+}
+
+void launch_gather_c(const float2 *f, const uint32_t *perm, long long M, float2 *fs, cudaStream_t s)
+{
+  if (M <= 0) return;
+  k_gather_c<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(f, perm, M, fs);
+  GB_LAUNCHED("gather_c");
+}
+
+}  // namespace gb

@@ -150,7 +150,21 @@ __device__ __forceinline__ float kb_phi_t_fast(float t, float mm, float b)
 
 __device__ __forceinline__ float kb_window_t(float t, float mm, float b) { return kb_phi_t_fast(t, mm, b); }
 
-// the W taps of a node from its polynomial form: t0 = n x - u in [m, m+1)
+// the W taps of a node from its polynomial form, s = 2 frac(n x) - 1
+template <int W>
+__device__ __forceinline__ void kb_poly_taps_s(float s, const float (&c)[KB_POLY_WMAX][KB_POLY_DP], float (&v)[W])
+{
+  static_assert(W <= KB_POLY_WMAX, "no polynomial form for this width");
+#pragma unroll
+  for (int l = 0; l < W; ++l) {
+    float a = c[l][KB_POLY_DP - 1];
+#pragma unroll
+    for (int k = KB_POLY_DP - 2; k >= 0; --k) a = fmaf(a, s, c[l][k]);
+    v[l] = a;
+  }
+}
+
+// the same from t0 = n x - u in [m, m+1)
 template <int W>
 __device__ __forceinline__ void kb_poly_taps(float t0, int m, const float (&c)[KB_POLY_WMAX][KB_POLY_DP],
                                              float (&v)[W])

@@ -74,15 +74,25 @@ int group3_subcell_edge();
 // z-column B^T kernel (nodes keyed by (x sub-cell, y sub-cell, z cell))
 template <typename R>
 bool group3_column_supported(int w);
+// node-set data of the single-precision column / sub-cell kernels
+struct Col3Bufs {
+  const float4 *rec;    // per sorted node: s_0, s_1, s_2, packed window starts in the tile
+  const uint16_t *cst;  // per work item: 17 column starts
+  const uint16_t *sst;  // per work item: 65 sub-cell starts
+  float2 *fs;           // adjoint input in tile order (M values)
+};
+void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *items, int nitems,
+                     const uint32_t *keys, float4 *rec, uint16_t *cst, uint16_t *sst, cudaStream_t s);
+void launch_gather_c(const float2 *f, const uint32_t *perm, long long M, float2 *fs, cudaStream_t s);
 int group3_max_item();
 template <typename R>
 void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
                      const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
-                     cudaStream_t s);
+                     const Col3Bufs &cb, cudaStream_t s);
 template <typename R>
 void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
                       const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
-                      cudaStream_t s);
+                      const Col3Bufs &cb, cudaStream_t s);
 // generic global-memory kernels for any d and m
 template <typename R>
 void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,

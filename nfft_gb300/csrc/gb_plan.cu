@@ -18,6 +18,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -70,6 +71,10 @@ struct Ctx {
   bool tiled = false;
   bool group3 = false;  // 3-D sub-cell group kernels
   WinPoly poly = {};     // polynomial window of the single-precision 3-D kernels
+  bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
+  float4 *c3rec = nullptr;
+  uint16_t *c3cst = nullptr, *c3sst = nullptr;
+  C *fs = nullptr;       // adjoint input in tile order
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // FFT: one plan for d <= 3; for d > 3 a rank-3 plan over the last three
@@ -394,6 +399,14 @@ static void init_help(typename Api<R>::plan *ths)
     dev_alloc<R>((void **)&c->tile_start, ((size_t)c->ntiles + 1) * sizeof(uint32_t));
     const int chunk = 1024;
     dev_alloc<R>((void **)&c->items, ((size_t)c->ntiles + M / chunk + 2) * sizeof(WorkItem));
+    c->col3 = c->group3 && sizeof(R) == 4 && group3_column_supported<R>(g.w);
+    if (c->col3) {
+      const size_t cap = (size_t)c->ntiles + M / chunk + 2;
+      dev_alloc<R>((void **)&c->c3rec, M * sizeof(float4));
+      dev_alloc<R>((void **)&c->c3cst, cap * 17 * sizeof(uint16_t));
+      dev_alloc<R>((void **)&c->c3sst, cap * 65 * sizeof(uint16_t));
+      dev_alloc<R>((void **)&c->fs, M * sizeof(C));
+    }
     make_fft<R>(c);
   }
   launch_cphi<R>(g, c->cphi, c->stream);
@@ -473,6 +486,8 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
     c->nitems = c->tiled ? build_work_items(c->tile_start, c->ntiles, chunk, c->items, cnt, off,
                                             total, temp, s)
                          : 0;
+    if constexpr (std::is_same<R, float>::value)
+      if (c->col3) launch_c3_setup(c->xs, g, c->items, c->nitems, k1, c->c3rec, c->c3cst, c->c3sst, s);
     if (cnt != k2) {
       GB_CUDA(cudaFree(cnt));
       GB_CUDA(cudaFree(off));
@@ -521,9 +536,20 @@ static void ensure_nodes(typename Api<R>::plan *ths, Ctx<R> *c)
 // memset of B^T, ev[2] stage 1 end, ev[3] FFT end, ev[4] stage 3 end,
 // ev[5] call end (after the result copy).
 template <typename R>
+static Col3Bufs col3_bufs(Ctx<R> *c)
+{
+  Col3Bufs b;
+  b.rec = c->c3rec;
+  b.cst = c->c3cst;
+  b.sst = c->c3sst;
+  b.fs = reinterpret_cast<float2 *>(c->fs);
+  return b;
+}
+
+template <typename R>
 static void b_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
-  if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
+  if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, col3_bufs(c), c->stream);
   else if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_b_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
@@ -543,7 +569,7 @@ static void bt_stage(Ctx<R> *c, const typename Cx<R>::T *f, cudaEvent_t *E)
 {
   GB_CUDA(cudaMemsetAsync(c->grid, 0, (size_t)c->g.n_total * sizeof(typename Cx<R>::T), c->stream));
   GB_CUDA(cudaEventRecord(E[6], c->stream));
-  if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
+  if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, col3_bufs(c), c->stream);
   else if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_bt_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
@@ -787,6 +813,10 @@ static void finalize(typename Api<R>::plan *ths)
     cudaFree(c->cphi);
     cudaFree(c->tile_start);
     cudaFree(c->items);
+    cudaFree(c->c3rec);
+    cudaFree(c->c3cst);
+    cudaFree(c->c3sst);
+    cudaFree(c->fs);
     for (int i = 0; i < 7; ++i)
       if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (cudaEvent_t e : c->ring) cudaEventDestroy(e);

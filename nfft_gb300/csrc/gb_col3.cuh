@@ -54,10 +54,10 @@ struct C3 {
   static constexpr int RPL = 2;                              // rows a lane holds at once
   static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
   // per-warp scratch (floats): x scaled by f [CHUNK][BOXP] complex, y
-  // [CHUNK][BOXP], z duplicated [CHUNK][W] pairs
+  // duplicated [CHUNK][BOXP] pairs, z duplicated [CHUNK][W] pairs
   static constexpr int WXF = 0;
   static constexpr int WY = WXF + 2 * BOXP * C3_CHUNK;
-  static constexpr int WZ = WY + BOXP * C3_CHUNK;
+  static constexpr int WZ = WY + 2 * BOXP * C3_CHUNK;
   static constexpr int WARP_FLOATS = WZ + 2 * W * C3_CHUNK;
   static constexpr int INTS = 17 + 1;                        // column starts, task counter
   static_assert(BOXP > BOX, "x / y vectors need one zero slot past the column");
@@ -74,37 +74,43 @@ inline size_t c3_smem_bytes(const Geom<float> &g)
 
 __device__ __forceinline__ unsigned long long f2_bits(float2 v)
 {
-  return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
-}
-__device__ __forceinline__ float2 bits_f2(unsigned long long b)
-{
-  return make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32)));
+  union {
+    float2 f;
+    unsigned long long u;
+  } c;
+  c.f = v;
+  return c.u;
 }
 
-// Adds v[z] to the interleaved complex cells p[z] for z in [z1, z2) (a
-// warp-uniform range), ZB cells at a time: every cell of a block is read,
-// summed and offered by one 64-bit compare-and-swap before any result is
-// checked; a cell whose swap found a value changed by another warp in
-// between is added again with the atomic add of each component.
+// Adds v[z] to the interleaved complex cells p[z], z < N, ZB cells at a time
+// (blocks wholly outside the warp-uniform range [z1, z2) hold zeros and are
+// skipped):
+// every cell of a block is read, summed (one paired add) and offered by one
+// 64-bit compare-and-swap before any result is checked; a cell whose swap
+// found a value changed by another warp in between is added again with the
+// atomic add of each component.
 template <int N, int ZB>
 __device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&v)[N], int z1, int z2)
 {
+  volatile float2 *vp = p;
 #pragma unroll
   for (int z0 = 0; z0 < N; z0 += ZB) {
-    unsigned long long cur[ZB];
+    if (z0 + ZB <= z1 || z0 >= z2) continue;
+    float2 cur[ZB];
 #pragma unroll
-    for (int e = 0; e < ZB; ++e) {
-      const int z = z0 + e;
-      if (z < N && z >= z1 && z < z2) cur[e] = *reinterpret_cast<volatile unsigned long long *>(p + z);
-    }
+    for (int e = 0; e < ZB; ++e)
+      if (z0 + e < N) {
+        const volatile float2 &c = vp[z0 + e];
+        cur[e] = make_float2(c.x, c.y);
+      }
     unsigned miss = 0;
 #pragma unroll
     for (int e = 0; e < ZB; ++e) {
       const int z = z0 + e;
-      if (z < N && z >= z1 && z < z2) {
-        const float2 o = bits_f2(cur[e]);
-        const unsigned long long want = f2_bits(make_float2(o.x + v[z].x, o.y + v[z].y));
-        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z), cur[e], want) != cur[e]) miss |= 1u << e;
+      if (z < N) {
+        const unsigned long long old = f2_bits(cur[e]);
+        const unsigned long long want = f2_bits(__fadd2_rn(cur[e], v[z]));
+        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z), old, want) != old) miss |= 1u << e;
       }
     }
     if (miss) {
@@ -135,7 +141,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float *const wsc = base + warp * P::WARP_FLOATS;
   float2 *const wxf = reinterpret_cast<float2 *>(wsc + P::WXF);
-  float *const wy = wsc + P::WY;
+  float2 *const wy2 = reinterpret_cast<float2 *>(wsc + P::WY);
   float2 *const wz2 = reinterpret_cast<float2 *>(wsc + P::WZ);
   float2 *const sg = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
   int *const cstart = reinterpret_cast<int *>(sg + EXT * g.sx2);
@@ -215,19 +221,19 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       const int oy = ((loc >> 3) & 7) - 2 * s1;
       kb_poly_taps_s<W>(r.y, poly.c[1], v);
       {
-        float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
+        float4 *dst = reinterpret_cast<float4 *>(wy2 + lane * BOXP);
 #pragma unroll
-        for (int q = 0; q < BOXP / 4; ++q) {
-          float e[4];
+        for (int q = 0; q < BOXP / 2; ++q) {
+          float e[2];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int b = 4 * q + h;
+          for (int h = 0; h < 2; ++h) {
+            const int b = 2 * q + h;
             float val = 0.f;
             if (b < W && oy == 0) val = v[b];
             if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
             e[h] = val;
           }
-          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+          dst[q] = make_float4(e[0], e[0], e[1], e[1]);
         }
       }
       z0 = loc >> 6;
@@ -242,14 +248,9 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     int rs[9];
 #pragma unroll
     for (int z = 0; z <= 8; ++z) rs[z] = __popc(__ballot_sync(0xffffffffu, z0 < z));
+    // z range the chunk touches: first z0 .. last z0 + W
+    const int zlo = __shfl_sync(0xffffffffu, z0, 0), zhi = __shfl_sync(0xffffffffu, z0, np - 1) + W;
     __syncwarp();
-    int zmin = 8, zmax = -1;
-#pragma unroll
-    for (int z = 0; z < 8; ++z)
-      if (rs[z + 1] > rs[z]) {
-        zmin = min(zmin, z);
-        zmax = z;
-      }
 
 #pragma unroll 1
     for (int ri = 0; ri < P::RITER; ++ri) {
@@ -282,9 +283,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
           }
 #pragma unroll
           for (int q = 0; q < RPL; ++q) {
-            const float2 xf = wxf[j * BOXP + bx[q]];
-            const float yv = wy[j * BOXP + by[q]];
-            const float2 h = make_float2(xf.x * yv, xf.y * yv);
+            const float2 h = __fmul2_rn(wxf[j * BOXP + bx[q]], wy2[j * BOXP + by[q]]);
 #pragma unroll
             for (int z = 0; z < W; ++z) acc[q][zz + z] = __ffma2_rn(w[z], h, acc[q][zz + z]);
           }
@@ -292,7 +291,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       }
 #pragma unroll
       for (int q = 0; q < RPL; ++q)
-        if (ok[q]) c3_flush_row<EXT, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, acc[q], zmin, zmax + W);
+        if (ok[q]) c3_flush_row<EXT, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, acc[q], zlo, zhi);
     }
     __syncwarp();
   }
@@ -479,10 +478,20 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
         wbx[qq] = ok ? bx : BOXP - 1;  // rows past the box take the zero slot of the x vector
         const float *pr = sre + sbase + bx * g.sx + by[qq] * g.sy;
         const float *pi = sim + sbase + bx * g.sx + by[qq] * g.sy;
+        // row starts are even (even plane strides, even sub-cell z origin):
+        // pairs of z values load as 8-byte words
 #pragma unroll
-        for (int z = 0; z < BOX; ++z) {
-          gr[qq][z] = pr[z];
-          gi[qq][z] = pi[z];
+        for (int z = 0; z + 1 < BOX; z += 2) {
+          const float2 a = *reinterpret_cast<const float2 *>(pr + z);
+          const float2 b = *reinterpret_cast<const float2 *>(pi + z);
+          gr[qq][z] = a.x;
+          gr[qq][z + 1] = a.y;
+          gi[qq][z] = b.x;
+          gi[qq][z + 1] = b.y;
+        }
+        if (BOX & 1) {
+          gr[qq][BOX - 1] = pr[BOX - 1];
+          gi[qq][BOX - 1] = pi[BOX - 1];
         }
       }
 #pragma unroll

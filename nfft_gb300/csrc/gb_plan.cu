@@ -180,8 +180,9 @@ static void choose_tiles(Ctx<R> *c)
       int best = 1 << 30;
       g.sy = ext;
       g.sx = ext * ext;
-      for (int sy = ext; sy < ext + 8; ++sy)
-        for (int sx = ext * sy; sx < ext * sy + 40; ++sx) {
+      // (even strides: the sub-cell kernel reads rows as 8-byte pairs)
+      for (int sy = ext + (ext & 1); sy < ext + 8; sy += 2)
+        for (int sx = ext * sy; sx < ext * sy + 40; sx += 2) {
           int cost = 0;
           for (int r0 = 0; r0 < rows; r0 += 32) {
             int cnt[32] = {0}, worst = 0;

@@ -53,15 +53,17 @@ struct C3 {
   static constexpr int ROWS = BOX * BOX;                     // (x, y) rows of a column
   static constexpr int RPL = 2;                              // rows a lane holds at once
   static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
+  static constexpr int ZP = (W + 2 + 3) / 4 * 4;            // z taps with a parity shift, padded
+  static constexpr int NPAIR = (EXT + 1) / 2;                // z pairs of a row's accumulators
   // per-warp scratch (floats): x scaled by f [CHUNK][BOXP] complex, y
-  // duplicated [CHUNK][BOXP] pairs, z duplicated [CHUNK][W] pairs
+  // [CHUNK][BOXP], z [CHUNK][ZP] shifted by the parity of the window start
   static constexpr int WXF = 0;
   static constexpr int WY = WXF + 2 * BOXP * C3_CHUNK;
-  static constexpr int WZ = WY + 2 * BOXP * C3_CHUNK;
-  static constexpr int WARP_FLOATS = WZ + 2 * W * C3_CHUNK;
+  static constexpr int WZ = WY + BOXP * C3_CHUNK;
+  static constexpr int WARP_FLOATS = WZ + ZP * C3_CHUNK;
   static constexpr int INTS = 17 + 1;                        // column starts, task counter
   static_assert(BOXP > BOX, "x / y vectors need one zero slot past the column");
-  static_assert((2 * W) % 4 == 0, "z pair vectors are read four floats at a time");
+  static_assert(W % 2 == 0, "even window width");
 };
 
 template <int W>
@@ -89,39 +91,40 @@ __device__ __forceinline__ unsigned long long f2_bits(float2 v)
 // 64-bit compare-and-swap before any result is checked; a cell whose swap
 // found a value changed by another warp in between is added again with the
 // atomic add of each component.
-template <int N, int ZB>
-__device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&v)[N], int z1, int z2)
+template <int N, int NP, int ZB>
+__device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&vr)[NP], const float2 (&vi)[NP], int z1,
+                                             int z2)
 {
+  static_assert(N <= 2 * NP, "cells past the accumulators");
   volatile float2 *vp = p;
 #pragma unroll
   for (int z0 = 0; z0 < N; z0 += ZB) {
     if (z0 + ZB <= z1 || z0 >= z2) continue;
-    float2 cur[ZB];
+    float2 cur[ZB], v[ZB];
 #pragma unroll
     for (int e = 0; e < ZB; ++e)
       if (z0 + e < N) {
-        const volatile float2 &c = vp[z0 + e];
+        const int z = z0 + e;
+        const volatile float2 &c = vp[z];
         cur[e] = make_float2(c.x, c.y);
+        v[e] = make_float2((z & 1) ? vr[z >> 1].y : vr[z >> 1].x, (z & 1) ? vi[z >> 1].y : vi[z >> 1].x);
       }
     unsigned miss = 0;
 #pragma unroll
     for (int e = 0; e < ZB; ++e) {
-      const int z = z0 + e;
-      if (z < N) {
+      if (z0 + e < N) {
         const unsigned long long old = f2_bits(cur[e]);
-        const unsigned long long want = f2_bits(__fadd2_rn(cur[e], v[z]));
-        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z), old, want) != old) miss |= 1u << e;
+        const unsigned long long want = f2_bits(__fadd2_rn(cur[e], v[e]));
+        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z0 + e), old, want) != old) miss |= 1u << e;
       }
     }
     if (miss) {
 #pragma unroll
-      for (int e = 0; e < ZB; ++e) {
-        const int z = z0 + e;
-        if (z < N && (miss >> e) & 1u) {
-          atomicAdd(&p[z].x, v[z].x);
-          atomicAdd(&p[z].y, v[z].y);
+      for (int e = 0; e < ZB; ++e)
+        if (z0 + e < N && (miss >> e) & 1u) {
+          atomicAdd(&p[z0 + e].x, v[e].x);
+          atomicAdd(&p[z0 + e].y, v[e].y);
         }
-      }
     }
   }
 }
@@ -141,8 +144,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float *const wsc = base + warp * P::WARP_FLOATS;
   float2 *const wxf = reinterpret_cast<float2 *>(wsc + P::WXF);
-  float2 *const wy2 = reinterpret_cast<float2 *>(wsc + P::WY);
-  float2 *const wz2 = reinterpret_cast<float2 *>(wsc + P::WZ);
+  float *const wy = wsc + P::WY;
+  float *const wz = wsc + P::WZ;
   float2 *const sg = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
   int *const cstart = reinterpret_cast<int *>(sg + EXT * g.sx2);
   int *const taskctr = cstart + 17;
@@ -221,27 +224,41 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       const int oy = ((loc >> 3) & 7) - 2 * s1;
       kb_poly_taps_s<W>(r.y, poly.c[1], v);
       {
-        float4 *dst = reinterpret_cast<float4 *>(wy2 + lane * BOXP);
+        float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
 #pragma unroll
-        for (int q = 0; q < BOXP / 2; ++q) {
-          float e[2];
+        for (int q = 0; q < BOXP / 4; ++q) {
+          float e[4];
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int b = 2 * q + h;
+          for (int h = 0; h < 4; ++h) {
+            const int b = 4 * q + h;
             float val = 0.f;
             if (b < W && oy == 0) val = v[b];
             if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
             e[h] = val;
           }
-          dst[q] = make_float4(e[0], e[0], e[1], e[1]);
+          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
         }
       }
       z0 = loc >> 6;
       kb_poly_taps_s<W>(r.z, poly.c[2], v);
       {
-        float4 *dst = reinterpret_cast<float4 *>(wz2 + lane * W);
+        // taps at the node's z offset within its aligned pair: a window
+        // starting at odd z0 begins in the second half of a pair
+        const int oz = z0 & 1;
+        float4 *dst = reinterpret_cast<float4 *>(wz + lane * P::ZP);
 #pragma unroll
-        for (int q = 0; q < W / 2; ++q) dst[q] = make_float4(v[2 * q], v[2 * q], v[2 * q + 1], v[2 * q + 1]);
+        for (int q = 0; q < P::ZP / 4; ++q) {
+          float e[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int b = 4 * q + h;
+            float val = 0.f;
+            if (b < W && oz == 0) val = v[b];
+            if (b >= 1 && b - 1 < W && oz == 1) val = v[b - 1];
+            e[h] = val;
+          }
+          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+        }
       }
     }
     // runs of equal z0 (the chunk is sorted by z0): rs[z] = first lane with z0 >= z
@@ -264,34 +281,45 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
         bx[q] = ok[q] ? row / P::BOX : BOXP - 1;
         by[q] = ok[q] ? row - (row / P::BOX) * P::BOX : 0;
       }
-      float2 acc[RPL][EXT];
+      // real and imaginary accumulators of the row's z values, as aligned pairs
+      float2 ar[RPL][P::NPAIR], ai[RPL][P::NPAIR];
 #pragma unroll
       for (int q = 0; q < RPL; ++q)
 #pragma unroll
-        for (int z = 0; z < EXT; ++z) acc[q][z] = make_float2(0.f, 0.f);
+        for (int z = 0; z < P::NPAIR; ++z) ar[q][z] = ai[q][z] = make_float2(0.f, 0.f);
 #pragma unroll
       for (int zz = 0; zz < 8; ++zz) {
+        // window start zz: taps in pairs zz/2 .. zz/2 + npr - 1
+        const int b = zz >> 1, npr = (zz & 1) ? W / 2 + 1 : W / 2;
 #pragma unroll 1
         for (int j = rs[zz]; j < rs[zz + 1]; ++j) {
-          float2 w[W];
-          const float4 *src = reinterpret_cast<const float4 *>(wz2 + j * W);
+          float2 w[P::ZP / 2];
+          const float4 *src = reinterpret_cast<const float4 *>(wz + j * P::ZP);
 #pragma unroll
-          for (int q = 0; q < W / 2; ++q) {
+          for (int q = 0; q < P::ZP / 4; ++q) {
             const float4 t = src[q];
             w[2 * q] = make_float2(t.x, t.y);
             w[2 * q + 1] = make_float2(t.z, t.w);
           }
 #pragma unroll
           for (int q = 0; q < RPL; ++q) {
-            const float2 h = __fmul2_rn(wxf[j * BOXP + bx[q]], wy2[j * BOXP + by[q]]);
+            const float2 xf = wxf[j * BOXP + bx[q]];
+            const float yv = wy[j * BOXP + by[q]];
+            const float hr = xf.x * yv, hi = xf.y * yv;
+            const float2 hr2 = make_float2(hr, hr), hi2 = make_float2(hi, hi);
 #pragma unroll
-            for (int z = 0; z < W; ++z) acc[q][zz + z] = __ffma2_rn(w[z], h, acc[q][zz + z]);
+            for (int k = 0; k < W / 2 + 1; ++k)
+              if (k < npr) {
+                ar[q][b + k] = __ffma2_rn(w[k], hr2, ar[q][b + k]);
+                ai[q][b + k] = __ffma2_rn(w[k], hi2, ai[q][b + k]);
+              }
           }
         }
       }
 #pragma unroll
       for (int q = 0; q < RPL; ++q)
-        if (ok[q]) c3_flush_row<EXT, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, acc[q], zlo, zhi);
+        if (ok[q]) c3_flush_row<EXT, P::NPAIR, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, ar[q],
+                                                  ai[q], zlo, zhi);
     }
     __syncwarp();
   }

@@ -328,7 +328,8 @@ def run_gpu(args, wl):
     sums = (C.c_float * 7)()
     counts = (C.c_int * 2)()
     end(pa, sums, counts)
-    launches = 4 * args.steps  # k_d_pad + k_b3_group (trafo), k_bt3_group + k_d_crop (adjoint)
+    # trafo: k_d_pad + k_b3_cell; adjoint: k_gather_c + k_bt3_col + k_d_crop (cuFFT not counted)
+    launches = 5 * args.steps
     if dist is not None:
         t = torch.tensor([ms_total], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -367,7 +368,7 @@ def run_gpu(args, wl):
              "adjoint_memset_ms": sums[3] / nA, "adjoint_BT_ms": sums[4] / nA,
              "adjoint_FFT_ms": sums[5] / nA, "adjoint_DT_ms": sums[6] / nA}
     b_ms, bt_ms = stage["trafo_B_ms"], stage["adjoint_BT_ms"]
-    kb, kbt = ("k_b3_group", "k_bt3_group") if wl["d"] == 3 else ("k_b_tiled", "k_bt_tiled")
+    kb, kbt = ("k_b3_cell", "k_bt3_col") if wl["d"] == 3 else ("k_b_tiled", "k_bt_tiled")
     dom, dom_ms = (kbt + " (B^T spreading)", bt_ms) if bt_ms >= b_ms else (kb + " (B interpolation)", b_ms)
     peaks, peak_kind = measured_peaks()
     bytes_b = algorithmic_bytes_B(wl)

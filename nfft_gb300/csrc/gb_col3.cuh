@@ -84,6 +84,19 @@ __device__ __forceinline__ unsigned long long f2_bits(float2 v)
   return c.u;
 }
 
+// Starts a bulk copy of the 16-byte aligned interior of [p, p + bytes) from
+// global memory into L2 (cp.async.bulk.prefetch, sm_90 and later): the
+// work item's node data arrive while the CTA stages its subgrid.
+__device__ __forceinline__ void c3_prefetch_l2(const void *p, long long bytes)
+{
+  const unsigned long long a = (unsigned long long)p;
+  const unsigned long long b = (a + 15) & ~15ull, e = (a + (unsigned long long)bytes) & ~15ull;
+  for (unsigned long long q = b; q < e; q += (1u << 20)) {
+    const unsigned n = (unsigned)((e - q) < (1u << 20) ? (e - q) : (1u << 20));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
+  }
+}
+
 // Adds v[z] to the interleaved complex cells p[z], z < N, ZB cells at a time
 // (blocks wholly outside the warp-uniform range [z1, z2) hold zeros and are
 // skipped):
@@ -159,6 +172,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       org[t] = (rem % g.ntile[t]) * 8;
       rem /= g.ntile[t];
     }
+  }
+  if (threadIdx.x == 0) {
+    c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
+    c3_prefetch_l2(fs + it.start, 8LL * (it.end - it.start));
   }
   for (int i = threadIdx.x; i < EXT * g.sx2; i += C3_THREADS) sg[i] = make_float2(0.f, 0.f);
   // column boundaries of the item (node set-up): cstart[c] = first node of column c
@@ -293,14 +310,13 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
         const int b = zz >> 1, npr = (zz & 1) ? W / 2 + 1 : W / 2;
 #pragma unroll 1
         for (int j = rs[zz]; j < rs[zz + 1]; ++j) {
+          // 8-byte broadcast reads: a warp-wide 16-byte read of one address
+          // costs four shared-memory wavefronts, an 8-byte read one
           float2 w[P::ZP / 2];
-          const float4 *src = reinterpret_cast<const float4 *>(wz + j * P::ZP);
+          const float2 *src = reinterpret_cast<const float2 *>(wz + j * P::ZP);
 #pragma unroll
-          for (int q = 0; q < P::ZP / 4; ++q) {
-            const float4 t = src[q];
-            w[2 * q] = make_float2(t.x, t.y);
-            w[2 * q + 1] = make_float2(t.z, t.w);
-          }
+          for (int k = 0; k < P::ZP / 2; ++k)
+            if (k < npr) w[k] = src[k];
 #pragma unroll
           for (int q = 0; q < RPL; ++q) {
             const float2 xf = wxf[j * BOXP + bx[q]];
@@ -409,6 +425,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       org[t] = (rem % g.ntile[t]) * 8;
       rem /= g.ntile[t];
     }
+  }
+  if (threadIdx.x == 0) {
+    c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
+    c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
   }
   // stage the padded subgrid; several grid loads in flight per thread
 #pragma unroll 4
@@ -527,14 +547,13 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
         if (jb < np) {
 #pragma unroll
           for (int j = jb; j < jb + 2; ++j) {
+            // 8-byte broadcast reads (one shared-memory wavefront each)
             float wzj[BOXP];
 #pragma unroll
-            for (int b = 0; b < BOXP; b += 4) {
-              const float4 t = *reinterpret_cast<const float4 *>(wz + j * BOXP + b);
+            for (int b = 0; b < BOX; b += 2) {
+              const float2 t = *reinterpret_cast<const float2 *>(wz + j * BOXP + b);
               wzj[b] = t.x;
               wzj[b + 1] = t.y;
-              wzj[b + 2] = t.z;
-              wzj[b + 3] = t.w;
             }
 #pragma unroll
             for (int qq = 0; qq < RPL; ++qq) {

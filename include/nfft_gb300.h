@@ -129,6 +129,15 @@ int nfft_gb_mlp_grad(const float *params, const float *feat, const float *target
 int nfft_gb_mlp_adam(float *params, const float *grad, float *m1, float *m2, int step, float lr,
                      float beta1, float beta2, float eps, void *stream);
 
+/* The polynomial form of the Kaiser-Bessel window that the single-precision
+ * 3-D kernels evaluate on the fly in place of the PRE_PSI table (reference
+ * window: include/infft.h:209-222).  For the window with cut-off m and shape
+ * b, coef[l * 10 + k] (l < w = 2m + 2, k < 10, host memory) is the k-th
+ * power coefficient of tap l as a polynomial in s = 2 frac(n x) - 1: the
+ * degree-9 interpolant, in double precision at the ten Chebyshev points of
+ * [-1, 1], of phi(n x - (u + l)) with u = floor(n x) - m.  Host only. */
+void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef);
+
 /* The node sort of NFFT_SORT_NODES without any device allocation (no
  * counterpart in the reference).  For callers that cannot allocate device
  * memory where they sort nodes: their memory belongs to a caching allocator

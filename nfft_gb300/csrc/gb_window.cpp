@@ -76,3 +76,5 @@ void kb_poly_fit(int m, double b, int w, float *coef)
 }
 
 }  // namespace gb
+
+extern "C" void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef) { gb::kb_poly_fit(m, b, w, coef); }

@@ -1,0 +1,56 @@
+"""The polynomial window of the single-precision 3-D kernels, checked on the
+CPU against the Kaiser-Bessel window of the reference (include/infft.h:209-222):
+phi(t) = sinh(b sqrt(m^2 - t^2)) / (pi sqrt(m^2 - t^2)) inside the support,
+sin(b sqrt(t^2 - m^2)) / (pi sqrt(t^2 - m^2)) outside, b / pi on its edge,
+with t = n x - (u + l) and b = pi (2 - 1 / sigma)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import nfft_gb300
+
+
+def kb_phi(t, m, b):
+    t = np.asarray(t, dtype=np.float64)
+    a = m * m - t * t
+    out = np.full_like(t, b / np.pi)
+    pos, neg = a > 0, a < 0
+    s = np.sqrt(a[pos])
+    out[pos] = np.sinh(b * s) / (np.pi * s)
+    s = np.sqrt(-a[neg])
+    out[neg] = np.sin(b * s) / (np.pi * s)
+    return out
+
+
+def horner_f32(c, s):
+    """Single-precision Horner evaluation, one rounding per multiply-add as the
+    kernels' fused multiply-adds (computed in double, rounded to float)."""
+    s64 = s.astype(np.float32).astype(np.float64)
+    v = np.full(s.shape, np.float32(c[-1]), dtype=np.float32)
+    for k in range(len(c) - 2, -1, -1):
+        v = (v.astype(np.float64) * s64 + np.float64(np.float32(c[k]))).astype(np.float32)
+    return v.astype(np.float64)
+
+
+@pytest.mark.parametrize("m,sigma", [(2, 2.0), (3, 2.0), (4, 2.0), (4, 1.5), (4, 1.25), (3, 1.25)])
+def test_polynomial_window_matches_kaiser_bessel(m, sigma):
+    lib = nfft_gb300.lib()
+    fit = lib.nfft_gb_kb_poly_fit
+    fit.restype = None
+    fit.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_float)]
+    w = 2 * m + 2
+    b = float(np.float32(np.pi * (2.0 - 1.0 / sigma)))  # the plan keeps b in its precision
+    coef = (C.c_float * (w * 10))()
+    fit(m, b, w, coef)
+    c = np.ctypeslib.as_array(coef).reshape(w, 10)
+    rng = np.random.default_rng(m)
+    frac = np.concatenate([rng.uniform(0, 1, 2000), [0.0, 0.5, 1.0 - 2.0 ** -24]])
+    s = 2.0 * frac - 1.0
+    peak = kb_phi(np.array([0.0]), m, b)[0]
+    worst = 0.0
+    for l in range(w):
+        exact = kb_phi(frac + m - l, m, b)
+        worst = max(worst, np.max(np.abs(horner_f32(c[l], s) - exact)) / peak)
+    # single-precision rounding of the window's peak is 6e-8 of it
+    assert worst < 2e-7, worst

@@ -168,7 +168,34 @@ NFFT_EXTERN void X(init_advanced_complex)(X(plan_complex)* ths, Y(mv_plan_comple
 NFFT_EXTERN void X(init_complex)(X(plan_complex)* ths, Y(mv_plan_complex) *mv); \
 NFFT_EXTERN void X(before_loop_complex)(X(plan_complex)* ths); \
 NFFT_EXTERN void X(loop_one_step_complex)(X(plan_complex) *ths); \
-NFFT_EXTERN void X(finalize_complex)(X(plan_complex) *ths);
+NFFT_EXTERN void X(finalize_complex)(X(plan_complex) *ths); \
+/* reference include/nfft3.h:788-815: the same solver over a real operator */ \
+typedef struct \
+{ \
+  Y(mv_plan_double) *mv; \
+  unsigned flags; \
+  R *w; \
+  R *w_hat; \
+  R *y; \
+  R *f_hat_iter; \
+  R *r_iter; \
+  R *z_hat_iter; \
+  R *p_hat_iter; \
+  R *v_iter; \
+  R alpha_iter; \
+  R beta_iter; \
+  R dot_r_iter; \
+  R dot_r_iter_old; \
+  R dot_z_hat_iter; \
+  R dot_z_hat_iter_old; \
+  R dot_p_hat_iter; \
+  R dot_v_iter; \
+} X(plan_double); \
+NFFT_EXTERN void X(init_advanced_double)(X(plan_double)* ths, Y(mv_plan_double) *mv, unsigned flags); \
+NFFT_EXTERN void X(init_double)(X(plan_double)* ths, Y(mv_plan_double) *mv); \
+NFFT_EXTERN void X(before_loop_double)(X(plan_double)* ths); \
+NFFT_EXTERN void X(loop_one_step_double)(X(plan_double) *ths); \
+NFFT_EXTERN void X(finalize_double)(X(plan_double) *ths);
 
 SOLVER_DEFINE_API(SOLVER_MANGLE_FLOAT,NFFT_MANGLE_FLOAT,float,fftwf_complex)
 SOLVER_DEFINE_API(SOLVER_MANGLE_DOUBLE,NFFT_MANGLE_DOUBLE,double,fftw_complex)

@@ -121,6 +121,11 @@ nfft_mv_plan_complex = _mv_struct(C.c_double, "nfft_mv_plan_complex")
 nfftf_mv_plan_complex = _mv_struct(C.c_float, "nfftf_mv_plan_complex")
 solver_plan_complex = _solver_struct(C.c_double, nfft_mv_plan_complex, "solver_plan_complex")
 solverf_plan_complex = _solver_struct(C.c_float, nfftf_mv_plan_complex, "solverf_plan_complex")
+# the real-valued operator and solver (include/nfft3.h:67, 788-815)
+nfft_mv_plan_double = _mv_struct(C.c_double, "nfft_mv_plan_double")
+nfftf_mv_plan_double = _mv_struct(C.c_float, "nfftf_mv_plan_double")
+solver_plan_double = _solver_struct(C.c_double, nfft_mv_plan_double, "solver_plan_double")
+solverf_plan_double = _solver_struct(C.c_float, nfftf_mv_plan_double, "solverf_plan_double")
 
 
 class Precision:

@@ -72,7 +72,8 @@ LAYOUT_PROG = r"""
   F(T,p_hat_iter) F(T,v_iter) F(T,alpha_iter) F(T,beta_iter) F(T,dot_r_iter) F(T,dot_r_iter_old) \
   F(T,dot_z_hat_iter) F(T,dot_z_hat_iter_old) F(T,dot_p_hat_iter) F(T,dot_v_iter) \
   printf(#T " sizeof %zu\n", sizeof(T));
-int main(void) { PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex) return 0; }
+int main(void) { PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
+  SOLV(solver_plan_double) SOLV(solverf_plan_double) return 0; }
 """
 
 
@@ -90,7 +91,9 @@ def _ctypes_layout():
     out = {}
     for name, st in (("nfft_plan", abi.nfft_plan), ("nfftf_plan", abi.nfftf_plan),
                      ("solver_plan_complex", abi.solver_plan_complex),
-                     ("solverf_plan_complex", abi.solverf_plan_complex)):
+                     ("solverf_plan_complex", abi.solverf_plan_complex),
+                     ("solver_plan_double", abi.solver_plan_double),
+                     ("solverf_plan_double", abi.solverf_plan_double)):
         for f, _ in st._fields_:
             out[(name, f)] = getattr(st, f).offset
         out[(name, "sizeof")] = C.sizeof(st)

@@ -138,6 +138,57 @@ NFFT_DEFINE_API(NFFT_MANGLE_DOUBLE,FFTW_MANGLE_DOUBLE,double,fftw_complex)
 #define NFFT_OMP_BLOCKWISE_ADJOINT (1U<<12)
 #define PRE_ONE_PSI (PRE_LIN_PSI| PRE_FG_PSI| PRE_PSI| PRE_FULL_PSI)
 
+/* reference include/nfft3.h:375-440: NNFFT, nonequispaced nodes in both space
+ * and frequency (double precision, as the reference's kernel/nnfft/nnfft.c) */
+#define NNFFT_MANGLE_DOUBLE(name) NFFT_CONCAT(nnfft_, name)
+
+#define NNFFT_DEFINE_API(X,Z,R,C) \
+typedef struct \
+{ \
+  MACRO_MV_PLAN(C) \
+  int d; \
+  R *sigma; \
+  R *a; \
+  int *N; \
+  int *N1; \
+  int *aN1; \
+  int m; \
+  R *b; \
+  int K; \
+  int aN1_total; \
+  Z(plan) *direct_plan; \
+  unsigned nnfft_flags; \
+  int *n; \
+  R *x; \
+  R *v; \
+  R *c_phi_inv; \
+  R *psi; \
+  int size_psi; \
+  int *psi_index_g; \
+  int *psi_index_f; \
+  C *F; \
+  R *spline_coeffs; \
+} X(plan); \
+NFFT_EXTERN void X(init)(X(plan) *ths_plan, int d, int N_total, int M_total, int *N); \
+NFFT_EXTERN void X(init_1d)(X(plan) *ths_plan, int N, int M_total); \
+NFFT_EXTERN void X(init_guru)(X(plan) *ths_plan, int d, int N_total, int M_total, \
+  int *N, int *N1, int m, unsigned nnfft_flags); \
+NFFT_EXTERN void X(trafo_direct)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(adjoint_direct)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(trafo)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(adjoint)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(precompute_lin_psi)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(precompute_psi)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(precompute_full_psi)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(precompute_phi_hut)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(precompute_one_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(finalize)(X(plan) *ths_plan);
+
+NNFFT_DEFINE_API(NNFFT_MANGLE_DOUBLE,NFFT_MANGLE_DOUBLE,double,fftw_complex)
+
+/* reference include/nfft3.h:439: additional NNFFT init flag */
+#define MALLOC_V         (1U<< 11)
+
 /* reference include/nfft3.h:747-815: inverse NFFT solver */
 #define SOLVER_MANGLE_DOUBLE(name) NFFT_CONCAT(solver_, name)
 #define SOLVER_MANGLE_FLOAT(name) NFFT_CONCAT(solverf_, name)

@@ -121,6 +121,33 @@ nfft_mv_plan_complex = _mv_struct(C.c_double, "nfft_mv_plan_complex")
 nfftf_mv_plan_complex = _mv_struct(C.c_float, "nfftf_mv_plan_complex")
 solver_plan_complex = _solver_struct(C.c_double, nfft_mv_plan_complex, "solver_plan_complex")
 solverf_plan_complex = _solver_struct(C.c_float, nfftf_mv_plan_complex, "solverf_plan_complex")
+# the NNFFT plan (include/nfft3.h:387-432), double precision
+nnfft_plan = type("nnfft_plan", (C.Structure,), {"_fields_": _mv_fields(C.c_double) + [
+    ("d", C.c_int),
+    ("sigma", C.POINTER(C.c_double)),
+    ("a", C.POINTER(C.c_double)),
+    ("N", C.POINTER(C.c_int)),
+    ("N1", C.POINTER(C.c_int)),
+    ("aN1", C.POINTER(C.c_int)),
+    ("m", C.c_int),
+    ("b", C.POINTER(C.c_double)),
+    ("K", C.c_int),
+    ("aN1_total", C.c_int),
+    ("direct_plan", C.POINTER(nfft_plan)),
+    ("nnfft_flags", C.c_uint),
+    ("n", C.POINTER(C.c_int)),
+    ("x", C.POINTER(C.c_double)),
+    ("v", C.POINTER(C.c_double)),
+    ("c_phi_inv", C.POINTER(C.c_double)),
+    ("psi", C.POINTER(C.c_double)),
+    ("size_psi", C.c_int),
+    ("psi_index_g", C.POINTER(C.c_int)),
+    ("psi_index_f", C.POINTER(C.c_int)),
+    ("F", C.POINTER(C.c_double)),
+    ("spline_coeffs", C.POINTER(C.c_double)),
+]})
+MALLOC_V = 1 << 11
+
 # the real-valued operator and solver (include/nfft3.h:67, 788-815)
 nfft_mv_plan_double = _mv_struct(C.c_double, "nfft_mv_plan_double")
 nfftf_mv_plan_double = _mv_struct(C.c_float, "nfftf_mv_plan_double")

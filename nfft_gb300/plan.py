@@ -205,3 +205,51 @@ class Solver:
             self.finalize()
         except Exception:
             pass
+
+
+class NnPlan:
+    """An NNFFT plan (nonequispaced space and frequency nodes, double
+    precision) driven through the nnfft_* entry points of ``lib`` as C callers
+    of the reference do (reference kernel/nnfft/nnfft.c): init_guru, fill x
+    (M x d) and v (N_total x d), precompute_one_psi, fill f_hat or f,
+    trafo / adjoint (or their _direct forms), read the other vector."""
+
+    def __init__(self, lib, N, N_total, M, N1, m, flags):
+        self.lib = lib
+        self.d = len(N)
+        self.N_total, self.M = int(N_total), int(M)
+        self.p = abi.nnfft_plan()
+        for name in ("init_guru", "trafo", "adjoint", "trafo_direct", "adjoint_direct",
+                     "precompute_one_psi", "finalize"):
+            fn = getattr(lib, "nnfft_" + name)
+            fn.restype = None
+        Nc = (C.c_int * self.d)(*[int(v) for v in N])
+        N1c = (C.c_int * self.d)(*[int(v) for v in N1])
+        lib.nnfft_init_guru(C.byref(self.p), self.d, self.N_total, self.M, Nc, N1c, int(m), C.c_uint(flags))
+        self.x = _view(self.p.x, self.M * self.d, np.float64)
+        self.v = _view(self.p.v, self.N_total * self.d, np.float64)
+        self.f = _view(self.p.f, 2 * self.M, np.float64).view(np.complex128)
+        self.f_hat = _view(self.p.f_hat, 2 * self.N_total, np.float64).view(np.complex128)
+
+    def _call(self, name):
+        getattr(self.lib, "nnfft_" + name)(C.byref(self.p))
+
+    def precompute_one_psi(self):
+        self._call("precompute_one_psi")
+
+    def trafo(self):
+        self._call("trafo")
+
+    def adjoint(self):
+        self._call("adjoint")
+
+    def trafo_direct(self):
+        self._call("trafo_direct")
+
+    def adjoint_direct(self):
+        self._call("adjoint_direct")
+
+    def finalize(self):
+        if self.p is not None:
+            self._call("finalize")
+            self.p = None

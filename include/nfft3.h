@@ -189,6 +189,42 @@ NNFFT_DEFINE_API(NNFFT_MANGLE_DOUBLE,NFFT_MANGLE_DOUBLE,double,fftw_complex)
 /* reference include/nfft3.h:439: additional NNFFT init flag */
 #define MALLOC_V         (1U<< 11)
 
+/* reference include/nfft3.h:500-545: MRI operators with a field inhomogeneity
+ * (double precision, as the reference's kernel/mri/mri.c) */
+#define MRI_MANGLE_DOUBLE(name) NFFT_CONCAT(mri_, name)
+
+#define MRI_DEFINE_API(X,Z,R,C) \
+typedef struct \
+{ \
+  MACRO_MV_PLAN(C) \
+  Z(plan) plan; \
+  int N3; \
+  R sigma3; \
+  R *t; \
+  R *w; \
+} X(inh_2d1d_plan); \
+typedef struct \
+{ \
+  MACRO_MV_PLAN(C) \
+  Z(plan) plan; \
+  int N3; \
+  R sigma3; \
+  R *t; \
+  R *w; \
+} X(inh_3d_plan); \
+void X(inh_2d1d_trafo)(X(inh_2d1d_plan) *ths); \
+void X(inh_2d1d_adjoint)(X(inh_2d1d_plan) *ths); \
+void X(inh_2d1d_init_guru)(X(inh_2d1d_plan) *ths, int *N, int M, int *n, \
+  int m, R sigma, unsigned nfft_flags, unsigned fftw_flags); \
+void X(inh_2d1d_finalize)(X(inh_2d1d_plan) *ths); \
+void X(inh_3d_trafo)(X(inh_3d_plan) *ths); \
+void X(inh_3d_adjoint)(X(inh_3d_plan) *ths); \
+void X(inh_3d_init_guru)(X(inh_3d_plan) *ths, int *N, int M, int *n, \
+  int m, R sigma, unsigned nfft_flags, unsigned fftw_flags); \
+void X(inh_3d_finalize)(X(inh_3d_plan) *ths);
+
+MRI_DEFINE_API(MRI_MANGLE_DOUBLE,NFFT_MANGLE_DOUBLE,double,fftw_complex)
+
 /* reference include/nfft3.h:747-815: inverse NFFT solver */
 #define SOLVER_MANGLE_DOUBLE(name) NFFT_CONCAT(solver_, name)
 #define SOLVER_MANGLE_FLOAT(name) NFFT_CONCAT(solverf_, name)

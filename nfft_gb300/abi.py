@@ -148,6 +148,21 @@ nnfft_plan = type("nnfft_plan", (C.Structure,), {"_fields_": _mv_fields(C.c_doub
 ]})
 MALLOC_V = 1 << 11
 
+# the MRI operators (include/nfft3.h:510-540), double precision; both plan
+# types share one layout
+def _mri_struct(name):
+    return type(name, (C.Structure,), {"_fields_": _mv_fields(C.c_double) + [
+        ("plan", nfft_plan),
+        ("N3", C.c_int),
+        ("sigma3", C.c_double),
+        ("t", C.POINTER(C.c_double)),
+        ("w", C.POINTER(C.c_double)),
+    ]})
+
+
+mri_inh_2d1d_plan = _mri_struct("mri_inh_2d1d_plan")
+mri_inh_3d_plan = _mri_struct("mri_inh_3d_plan")
+
 # the real-valued operator and solver (include/nfft3.h:67, 788-815)
 nfft_mv_plan_double = _mv_struct(C.c_double, "nfft_mv_plan_double")
 nfftf_mv_plan_double = _mv_struct(C.c_float, "nfftf_mv_plan_double")

@@ -253,3 +253,58 @@ class NnPlan:
         if self.p is not None:
             self._call("finalize")
             self.p = None
+
+
+class MriPlan:
+    """An MRI operator with a field inhomogeneity (kind "2d1d" or "3d",
+    double precision) driven through the mri_inh_* entry points of ``lib``
+    (reference kernel/mri/mri.c): init_guru, fill plan.x (the k-space nodes,
+    M x 2 for 2d1d, M x 3 for 3d), nfft_precompute_one_psi on the embedded
+    plan, t (2d1d: sample times) and w (field map), then trafo / adjoint."""
+
+    def __init__(self, lib, kind, N, M, n, m, sigma, flags, fftw_flags=None):
+        self.lib, self.kind = lib, kind
+        self.M = int(M)
+        self.p = (abi.mri_inh_2d1d_plan if kind == "2d1d" else abi.mri_inh_3d_plan)()
+        pre = "mri_inh_%s_" % kind
+        self._fn = {k: getattr(lib, pre + k) for k in ("init_guru", "trafo", "adjoint", "finalize")}
+        for fn in self._fn.values():
+            fn.restype = None
+        self._fn["init_guru"].argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
+                                          C.c_double, C.c_uint, C.c_uint]
+        if fftw_flags is None:
+            fftw_flags = abi.FFTW_ESTIMATE | abi.FFTW_DESTROY_INPUT
+        d = 2 if kind == "2d1d" else 3
+        Nc = (C.c_int * 3)(*[int(v) for v in N])
+        nc = (C.c_int * d)(*[int(v) for v in n])
+        self._fn["init_guru"](C.addressof(self.p), Nc, self.M, nc, int(m), float(sigma), int(flags), int(fftw_flags))
+        self.N_total = int(self.p.N_total)
+        self.d = d
+        self.x = _view(self.p.plan.x, self.M * d, np.float64)
+        self.w = _view(self.p.w, self.N_total, np.float64)
+        self.t = _view(self.p.t, self.M, np.float64) if kind == "2d1d" else None
+        pc = getattr(lib, "nfft_precompute_one_psi")
+        pc.restype = None
+        self._precompute = pc
+
+    @property
+    def f(self):
+        return _view(self.p.f, 2 * self.M, np.float64).view(np.complex128)
+
+    @property
+    def f_hat(self):
+        return _view(self.p.f_hat, 2 * self.N_total, np.float64).view(np.complex128)
+
+    def precompute(self):
+        self._precompute(C.pointer(self.p.plan))  # the embedded plan, in place
+
+    def trafo(self):
+        self._fn["trafo"](C.c_void_p(C.addressof(self.p)))
+
+    def adjoint(self):
+        self._fn["adjoint"](C.c_void_p(C.addressof(self.p)))
+
+    def finalize(self):
+        if self.p is not None:
+            self._fn["finalize"](C.c_void_p(C.addressof(self.p)))
+            self.p = None

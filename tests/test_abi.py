@@ -33,6 +33,7 @@ def _declared_functions():
         "SOLVER_DEFINE_API": ["solver_", "solverf_"],
         "NFFT_DEFINE_UTIL_API": ["nfft_", "nfftf_"],
         "NNFFT_DEFINE_API": ["nnfft_"],
+        "MRI_DEFINE_API": ["mri_"],
     }
     for macro, prefixes in api.items():
         body = re.search(r"#define %s\(.*?\)(.*?)\n\n" % macro, text, re.S).group(1)
@@ -77,8 +78,11 @@ LAYOUT_PROG = r"""
   F(T,a) F(T,N) F(T,N1) F(T,aN1) F(T,m) F(T,b) F(T,K) F(T,aN1_total) F(T,direct_plan) F(T,nnfft_flags) F(T,n) \
   F(T,x) F(T,v) F(T,c_phi_inv) F(T,psi) F(T,size_psi) F(T,psi_index_g) F(T,psi_index_f) F(T,F) \
   F(T,spline_coeffs) printf(#T " sizeof %zu\n", sizeof(T));
+#define MRI(T) F(T,N_total) F(T,M_total) F(T,f_hat) F(T,f) F(T,mv_trafo) F(T,mv_adjoint) F(T,plan) F(T,N3) \
+  F(T,sigma3) F(T,t) F(T,w) printf(#T " sizeof %zu\n", sizeof(T));
 int main(void) { PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
-  SOLV(solver_plan_double) SOLV(solverf_plan_double) NN(nnfft_plan) return 0; }
+  SOLV(solver_plan_double) SOLV(solverf_plan_double) NN(nnfft_plan) MRI(mri_inh_2d1d_plan) MRI(mri_inh_3d_plan)
+  return 0; }
 """
 
 
@@ -99,7 +103,9 @@ def _ctypes_layout():
                      ("solverf_plan_complex", abi.solverf_plan_complex),
                      ("solver_plan_double", abi.solver_plan_double),
                      ("solverf_plan_double", abi.solverf_plan_double),
-                     ("nnfft_plan", abi.nnfft_plan)):
+                     ("nnfft_plan", abi.nnfft_plan),
+                     ("mri_inh_2d1d_plan", abi.mri_inh_2d1d_plan),
+                     ("mri_inh_3d_plan", abi.mri_inh_3d_plan)):
         for f, _ in st._fields_:
             out[(name, f)] = getattr(st, f).offset
         out[(name, "sizeof")] = C.sizeof(st)

@@ -148,6 +148,22 @@ nnfft_plan = type("nnfft_plan", (C.Structure,), {"_fields_": _mv_fields(C.c_doub
 ]})
 MALLOC_V = 1 << 11
 
+# the NFCT plan (include/nfft3.h:224-265), both precisions
+def _nfct_struct(R, name):
+    P = C.POINTER(R)
+    return type(name, (C.Structure,), {"_fields_": _mv_fields(R) + [
+        ("d", INT), ("N", C.POINTER(INT)), ("n", C.POINTER(INT)), ("n_total", INT),
+        ("sigma", P), ("m", INT), ("b", P), ("K", INT), ("flags", C.c_uint), ("fftw_flags", C.c_uint),
+        ("x", P), ("MEASURE_TIME_t", C.c_double * 3), ("my_fftw_r2r_plan", C.c_void_p),
+        ("r2r_kind", C.POINTER(C.c_int)), ("c_phi_inv", C.POINTER(P)), ("psi", P), ("size_psi", INT),
+        ("psi_index_g", C.POINTER(INT)), ("psi_index_f", C.POINTER(INT)),
+        ("g", P), ("g_hat", P), ("g1", P), ("g2", P), ("spline_coeffs", P),
+    ]})
+
+
+nfct_plan = _nfct_struct(C.c_double, "nfct_plan")
+nfctf_plan = _nfct_struct(C.c_float, "nfctf_plan")
+
 # the MRI operators (include/nfft3.h:510-540), double precision; both plan
 # types share one layout
 def _mri_struct(name):

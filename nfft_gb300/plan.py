@@ -308,3 +308,61 @@ class MriPlan:
         if self.p is not None:
             self._fn["finalize"](C.c_void_p(C.addressof(self.p)))
             self.p = None
+
+
+class TrigPlan:
+    """An NFCT plan (kind "nfct") driven through the nfct_* / nfctf_* entry
+    points of ``lib`` as C callers of the reference do (reference
+    kernel/nfct/nfct.c): init_guru, fill x (M x d in [0, 1/2)),
+    precompute_one_psi, fill f_hat (real, N_total) or f, trafo / adjoint or
+    their _direct forms."""
+
+    def __init__(self, lib, kind, single, N, M, n, m, flags, fftw_flags=None):
+        self.lib = lib
+        self.pfx = kind + ("f_" if single else "_")
+        self.dt = np.float32 if single else np.float64
+        self.p = (getattr(abi, kind + ("f_plan" if single else "_plan")))()
+        self.d = len(N)
+        self.M = int(M)
+        if fftw_flags is None:
+            fftw_flags = abi.FFTW_ESTIMATE | abi.FFTW_DESTROY_INPUT
+        fn = getattr(lib, self.pfx + "init_guru")
+        fn.restype = None
+        fn.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
+                       C.c_uint, C.c_uint]
+        Nc = (C.c_int * self.d)(*[int(v) for v in N])
+        nc = (C.c_int * self.d)(*[int(v) for v in n])
+        fn(C.addressof(self.p), self.d, Nc, self.M, nc, int(m), int(flags), int(fftw_flags))
+        self.N_total = int(self.p.N_total)
+        self.x = _view(self.p.x, self.M * self.d, self.dt)
+        self.f = _view(self.p.f, self.M, self.dt)
+        self.f_hat = _view(self.p.f_hat, self.N_total, self.dt)
+
+    def _call(self, name):
+        fn = getattr(self.lib, self.pfx + name)
+        fn.restype = C.c_char_p if name == "check" else None
+        return fn(C.c_void_p(C.addressof(self.p)))
+
+    def precompute_one_psi(self):
+        self._call("precompute_one_psi")
+
+    def trafo(self):
+        self._call("trafo")
+
+    def adjoint(self):
+        self._call("adjoint")
+
+    def trafo_direct(self):
+        self._call("trafo_direct")
+
+    def adjoint_direct(self):
+        self._call("adjoint_direct")
+
+    def check(self):
+        r = self._call("check")
+        return r.decode() if r else None
+
+    def finalize(self):
+        if self.p is not None:
+            self._call("finalize")
+            self.p = None

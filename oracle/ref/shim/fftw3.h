@@ -23,12 +23,16 @@ extern "C" {
 #define FFTW_PATIENT (1U << 5)
 #define FFTW_ESTIMATE (1U << 6)
 #define FFTW_WISDOM_ONLY (1U << 21)
+/* real-to-real kinds the reference's NFCT / NFST plan (FFTW's numbering) */
+#define FFTW_REDFT00 3
+#define FFTW_RODFT00 7
 #define ORACLE_FFTW_DECLARE(X, R) \
   typedef R _Complex X##complex; \
   typedef struct X##plan_s *X##plan; \
   typedef enum { X##R2HC_kind_ = 0 } X##r2r_kind_do_not_use; \
   typedef int X##r2r_kind; \
   X##plan X##plan_dft(int rank, const int *n, X##complex *in, X##complex *out, int sign, unsigned flags); \
+  X##plan X##plan_r2r(int rank, const int *n, R *in, R *out, const X##r2r_kind *kind, unsigned flags); \
   void X##execute(const X##plan p); \
   void X##destroy_plan(X##plan p); \
   void *X##malloc(size_t n); \

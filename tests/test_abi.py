@@ -34,6 +34,7 @@ def _declared_functions():
         "NFFT_DEFINE_UTIL_API": ["nfft_", "nfftf_"],
         "NNFFT_DEFINE_API": ["nnfft_"],
         "MRI_DEFINE_API": ["mri_"],
+        "NFCT_DEFINE_API": ["nfct_", "nfctf_"],
     }
     for macro, prefixes in api.items():
         body = re.search(r"#define %s\(.*?\)(.*?)\n\n" % macro, text, re.S).group(1)
@@ -80,7 +81,11 @@ LAYOUT_PROG = r"""
   F(T,spline_coeffs) printf(#T " sizeof %zu\n", sizeof(T));
 #define MRI(T) F(T,N_total) F(T,M_total) F(T,f_hat) F(T,f) F(T,mv_trafo) F(T,mv_adjoint) F(T,plan) F(T,N3) \
   F(T,sigma3) F(T,t) F(T,w) printf(#T " sizeof %zu\n", sizeof(T));
-int main(void) { PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
+#define CT(T) F(T,N_total) F(T,M_total) F(T,f_hat) F(T,f) F(T,mv_trafo) F(T,mv_adjoint) F(T,d) F(T,N) F(T,n) \
+  F(T,n_total) F(T,sigma) F(T,m) F(T,b) F(T,K) F(T,flags) F(T,fftw_flags) F(T,x) F(T,MEASURE_TIME_t) \
+  F(T,my_fftw_r2r_plan) F(T,r2r_kind) F(T,c_phi_inv) F(T,psi) F(T,size_psi) F(T,psi_index_g) \
+  F(T,psi_index_f) F(T,g) F(T,g_hat) F(T,g1) F(T,g2) F(T,spline_coeffs) printf(#T " sizeof %zu\n", sizeof(T));
+int main(void) { CT(nfct_plan) CT(nfctf_plan) PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
   SOLV(solver_plan_double) SOLV(solverf_plan_double) NN(nnfft_plan) MRI(mri_inh_2d1d_plan) MRI(mri_inh_3d_plan)
   return 0; }
 """
@@ -105,7 +110,8 @@ def _ctypes_layout():
                      ("solverf_plan_double", abi.solverf_plan_double),
                      ("nnfft_plan", abi.nnfft_plan),
                      ("mri_inh_2d1d_plan", abi.mri_inh_2d1d_plan),
-                     ("mri_inh_3d_plan", abi.mri_inh_3d_plan)):
+                     ("mri_inh_3d_plan", abi.mri_inh_3d_plan),
+                     ("nfct_plan", abi.nfct_plan), ("nfctf_plan", abi.nfctf_plan)):
         for f, _ in st._fields_:
             out[(name, f)] = getattr(st, f).offset
         out[(name, "sizeof")] = C.sizeof(st)

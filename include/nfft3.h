@@ -245,6 +245,63 @@ NFFT_EXTERN void X(finalize)(X(plan) *ths_plan);
 NFCT_DEFINE_API(NFCT_MANGLE_FLOAT,FFTW_MANGLE_FLOAT,float,fftwf_complex)
 NFCT_DEFINE_API(NFCT_MANGLE_DOUBLE,FFTW_MANGLE_DOUBLE,double,fftw_complex)
 
+/* reference include/nfft3.h:290-355: NFST, the nonequispaced fast sine
+ * transform, f_j = sum_{1 <= k < N} f_hat_{k-1} prod_t sin(2 pi k_t x_jt),
+ * nodes x in [0, 1/2]^d */
+#define NFST_MANGLE_DOUBLE(name) NFFT_CONCAT(nfst_, name)
+#define NFST_MANGLE_FLOAT(name) NFFT_CONCAT(nfstf_, name)
+
+#define NFST_DEFINE_API(X,Y,R,C) \
+typedef struct \
+{ \
+  MACRO_MV_PLAN(R) \
+  NFFT_INT d; \
+  NFFT_INT *N; \
+  NFFT_INT *n; \
+  NFFT_INT n_total; \
+  R *sigma; \
+  NFFT_INT m; \
+  R *b; \
+  NFFT_INT K; \
+  unsigned flags; \
+  unsigned fftw_flags; \
+  R *x; \
+  double MEASURE_TIME_t[3]; \
+  Y(plan) my_fftw_r2r_plan; \
+  Y(r2r_kind) *r2r_kind; \
+  R **c_phi_inv; \
+  R *psi; \
+  NFFT_INT size_psi; \
+  NFFT_INT *psi_index_g; \
+  NFFT_INT *psi_index_f; \
+  R *g; \
+  R *g_hat; \
+  R *g1; \
+  R *g2; \
+  R *spline_coeffs; \
+  R X(full_psi_eps); \
+} X(plan); \
+NFFT_EXTERN void X(init_1d)(X(plan) *ths_plan, int N0, int M_total); \
+NFFT_EXTERN void X(init_2d)(X(plan) *ths_plan, int N0, int N1, int M_total); \
+NFFT_EXTERN void X(init_3d)(X(plan) *ths_plan, int N0, int N1, int N2, int M_total); \
+NFFT_EXTERN void X(init)(X(plan) *ths_plan, int d, int *N, int M_total); \
+NFFT_EXTERN void X(init_guru)(X(plan) *ths_plan, int d, int *N, int M_total, int *n, \
+  int m, unsigned flags, unsigned fftw_flags); \
+NFFT_EXTERN void X(precompute_one_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(precompute_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(precompute_full_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(precompute_fg_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(precompute_lin_psi)(X(plan) *ths); \
+NFFT_EXTERN void X(trafo)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(trafo_direct)(const X(plan) *ths_plan); \
+NFFT_EXTERN void X(adjoint)(X(plan) *ths_plan); \
+NFFT_EXTERN void X(adjoint_direct)(const X(plan) *ths_plan); \
+NFFT_EXTERN const char* X(check)(X(plan) *ths); \
+NFFT_EXTERN void X(finalize)(X(plan) *ths_plan);
+
+NFST_DEFINE_API(NFST_MANGLE_FLOAT,FFTW_MANGLE_FLOAT,float,fftwf_complex)
+NFST_DEFINE_API(NFST_MANGLE_DOUBLE,FFTW_MANGLE_DOUBLE,double,fftw_complex)
+
 /* reference include/nfft3.h:500-545: MRI operators with a field inhomogeneity
  * (double precision, as the reference's kernel/mri/mri.c) */
 #define MRI_MANGLE_DOUBLE(name) NFFT_CONCAT(mri_, name)

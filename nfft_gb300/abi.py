@@ -149,7 +149,7 @@ nnfft_plan = type("nnfft_plan", (C.Structure,), {"_fields_": _mv_fields(C.c_doub
 MALLOC_V = 1 << 11
 
 # the NFCT plan (include/nfft3.h:224-265), both precisions
-def _nfct_struct(R, name):
+def _nfct_struct(R, name, extra=()):
     P = C.POINTER(R)
     return type(name, (C.Structure,), {"_fields_": _mv_fields(R) + [
         ("d", INT), ("N", C.POINTER(INT)), ("n", C.POINTER(INT)), ("n_total", INT),
@@ -158,11 +158,14 @@ def _nfct_struct(R, name):
         ("r2r_kind", C.POINTER(C.c_int)), ("c_phi_inv", C.POINTER(P)), ("psi", P), ("size_psi", INT),
         ("psi_index_g", C.POINTER(INT)), ("psi_index_f", C.POINTER(INT)),
         ("g", P), ("g_hat", P), ("g1", P), ("g2", P), ("spline_coeffs", P),
-    ]})
+    ] + list(extra)})
 
 
 nfct_plan = _nfct_struct(C.c_double, "nfct_plan")
 nfctf_plan = _nfct_struct(C.c_float, "nfctf_plan")
+# the NFST plan (include/nfft3.h:299-343): the same layout and one more field
+nfst_plan = _nfct_struct(C.c_double, "nfst_plan", [("nfst_full_psi_eps", C.c_double)])
+nfstf_plan = _nfct_struct(C.c_float, "nfstf_plan", [("nfstf_full_psi_eps", C.c_float)])
 
 # the MRI operators (include/nfft3.h:510-540), double precision; both plan
 # types share one layout

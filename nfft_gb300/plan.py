@@ -311,9 +311,9 @@ class MriPlan:
 
 
 class TrigPlan:
-    """An NFCT plan (kind "nfct") driven through the nfct_* / nfctf_* entry
-    points of ``lib`` as C callers of the reference do (reference
-    kernel/nfct/nfct.c): init_guru, fill x (M x d in [0, 1/2)),
+    """An NFCT or NFST plan (kind "nfct" or "nfst") driven through the nfct_* / nfctf_* entry
+    points (or nfst_* / nfstf_*) of ``lib`` as C callers of the reference do
+    (reference kernel/nfct/nfct.c, kernel/nfst/nfst.c): init_guru, fill x (M x d in [0, 1/2)),
     precompute_one_psi, fill f_hat (real, N_total) or f, trafo / adjoint or
     their _direct forms."""
 

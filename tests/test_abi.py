@@ -35,6 +35,7 @@ def _declared_functions():
         "NNFFT_DEFINE_API": ["nnfft_"],
         "MRI_DEFINE_API": ["mri_"],
         "NFCT_DEFINE_API": ["nfct_", "nfctf_"],
+        "NFST_DEFINE_API": ["nfst_", "nfstf_"],
     }
     for macro, prefixes in api.items():
         body = re.search(r"#define %s\(.*?\)(.*?)\n\n" % macro, text, re.S).group(1)
@@ -85,7 +86,8 @@ LAYOUT_PROG = r"""
   F(T,n_total) F(T,sigma) F(T,m) F(T,b) F(T,K) F(T,flags) F(T,fftw_flags) F(T,x) F(T,MEASURE_TIME_t) \
   F(T,my_fftw_r2r_plan) F(T,r2r_kind) F(T,c_phi_inv) F(T,psi) F(T,size_psi) F(T,psi_index_g) \
   F(T,psi_index_f) F(T,g) F(T,g_hat) F(T,g1) F(T,g2) F(T,spline_coeffs) printf(#T " sizeof %zu\n", sizeof(T));
-int main(void) { CT(nfct_plan) CT(nfctf_plan) PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
+int main(void) { CT(nfct_plan) CT(nfctf_plan) CT(nfst_plan) CT(nfstf_plan) F(nfst_plan,nfst_full_psi_eps)
+  F(nfstf_plan,nfstf_full_psi_eps) PLAN(nfft_plan) PLAN(nfftf_plan) SOLV(solver_plan_complex) SOLV(solverf_plan_complex)
   SOLV(solver_plan_double) SOLV(solverf_plan_double) NN(nnfft_plan) MRI(mri_inh_2d1d_plan) MRI(mri_inh_3d_plan)
   return 0; }
 """
@@ -111,7 +113,8 @@ def _ctypes_layout():
                      ("nnfft_plan", abi.nnfft_plan),
                      ("mri_inh_2d1d_plan", abi.mri_inh_2d1d_plan),
                      ("mri_inh_3d_plan", abi.mri_inh_3d_plan),
-                     ("nfct_plan", abi.nfct_plan), ("nfctf_plan", abi.nfctf_plan)):
+                     ("nfct_plan", abi.nfct_plan), ("nfctf_plan", abi.nfctf_plan),
+                     ("nfst_plan", abi.nfst_plan), ("nfstf_plan", abi.nfstf_plan)):
         for f, _ in st._fields_:
             out[(name, f)] = getattr(st, f).offset
         out[(name, "sizeof")] = C.sizeof(st)

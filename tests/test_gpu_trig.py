@@ -1,4 +1,5 @@
-"""NFCT (reference kernel/nfct/nfct.c) on the GPU in both precisions, against
+"""NFCT and NFST (reference kernel/nfct/nfct.c, kernel/nfst/nfst.c) on the GPU
+in both precisions, against
 the reference's own outputs (tests/golden/nfct_ref.npz, written by
 tests/golden/make_trig_golden.py from the reference compiled in place):
 trafo, adjoint and the direct transforms; plus the reference's check strings."""
@@ -57,3 +58,26 @@ def test_trig_fixture_pins_reference():
         lim = 1e-5 if single else 1e-7
         assert rel(z[name + "/trafo"], z[name + "/trafo_direct"]) < lim
         assert rel(z[name + "/adjoint"], z[name + "/adjoint_direct"]) < lim
+
+
+def test_nfst_openmp_direct_adjoint_quirk():
+    """CPU: the reference's OpenMP multivariate NFST adjoint_direct
+    (kernel/nfst/nfst.c:188-209) splits the flat index k_L by N_t rather than by
+    the N_t - 1 sine frequencies; the fixture keeps its output, which this
+    restatement of that split reproduces, and the GPU library follows formula
+    (1.2) instead (the serial branch, nfst.c:210-246)."""
+    z = np.load(os.path.join(GOLD, "nfct_ref.npz"))
+    for name, kind, single, N, M, n, m in mk.CASES:
+        if kind != "nfst" or len(N) == 1:
+            continue
+        x = z[name + "/x"].astype(np.float64).reshape(M, len(N))
+        f = z[name + "/f"].astype(np.float64)
+        NT = int(np.prod([v - 1 for v in N]))
+        k = np.zeros((NT, len(N)), np.int64)
+        rem = np.arange(NT)
+        for t in range(len(N) - 1, -1, -1):
+            k[:, t] = rem % N[t] + 1
+            rem //= N[t]
+        A = np.prod(np.sin(2 * np.pi * k[None, :, :] * x[:, None, :]), axis=2)
+        assert rel(z[name + "/adjoint_direct_openmp"], A.T @ f) < (1e-5 if single else 1e-12)
+        assert rel(z[name + "/adjoint_direct_openmp"], z[name + "/adjoint_direct"]) > 0.1

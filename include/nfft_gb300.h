@@ -46,6 +46,9 @@ void X(gb_stage_times)(X(plan) *ths, float *ms4); \
 void X(gb_device_stage_times)(X(plan) *ths, float *ms4); \
 /* Kernel launches of the last transform (library kernels, not cuFFT). */ \
 int X(gb_last_launch_count)(X(plan) *ths); \
+/* Counter of node set-ups (precompute) of the plan: work captured against \
+ * its node order (a CUDA graph) is stale once this changes. */ \
+unsigned long long X(gb_generation)(X(plan) *ths); \
 /* Time up to max_calls following device transforms with CUDA events on the \
  * plan's stream, without synchronising between them.  timing_end waits for \
  * them and returns the number of calls timed; sums7 (ms) = trafo D, trafo \
@@ -72,7 +75,11 @@ int X(gb_sync)(X(plan_complex) *ths); \
 int X(gb_set_refresh)(X(plan_complex) *ths, int every); \
 /* Device copies of f_hat_iter (N_total complex) and y (M_total complex). */ \
 void *X(gb_device_f_hat_iter)(X(plan_complex) *ths); \
-void *X(gb_device_y)(X(plan_complex) *ths);
+void *X(gb_device_y)(X(plan_complex) *ths); \
+/* 1 (default): steepest descent, CGNR and CGNE steps replay a CUDA graph of \
+ * the step's launches, captured on first use and again after the plan's \
+ * nodes change; 0: launch them one by one.  The results are the same. */ \
+int X(gb_set_graphs)(X(plan_complex) *ths, int on);
 
 NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_DOUBLE)
 NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_FLOAT)

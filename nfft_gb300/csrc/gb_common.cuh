@@ -60,7 +60,7 @@ struct Geom {
 // Polynomial form of the Kaiser-Bessel window (single-precision 3-D
 // kernels): tap l of a node is sum_k c[t][l][k] s^k with s = 2 frac(n x) - 1.
 #define KB_POLY_DP 10    // coefficients per tap (degree 9)
-#define KB_POLY_WMAX 10  // widest window with a polynomial form
+#define KB_POLY_WMAX 16  // widest window with a polynomial form
 struct WinPoly {
   float c[3][KB_POLY_WMAX][KB_POLY_DP];  // per dimension, tap, increasing power of s
   int same;                              // every dimension has the same b (c[0] serves all)

@@ -93,6 +93,14 @@ template <typename R>
 void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
                       const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, const WinPoly &poly,
                       const Col3Bufs &cb, cudaStream_t s);
+// single-precision 2-D B^T and B by sub-cell columns (nodes keyed by (32^2 tile,
+// column of CX x-cells by 8 y-cells)); col2_column_width(w) = CX, 0 where
+// the width has no such kernel
+int col2_column_width(int w);
+void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
+void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
+                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
 // generic global-memory kernels for any d and m
 template <typename R>
 void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,

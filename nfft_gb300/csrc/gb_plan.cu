@@ -70,7 +70,8 @@ struct Ctx {
   bool direct = false;   // reference switches to the NDFT (nfft.c:5658-5665)
   bool tiled = false;
   bool group3 = false;  // 3-D sub-cell group kernels
-  WinPoly poly = {};     // polynomial window of the single-precision 3-D kernels
+  WinPoly poly = {};     // polynomial window of the single-precision 2-D / 3-D kernels
+  bool col2 = false;     // single-precision 2-D column B and B^T (nodes keyed by column)
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
@@ -99,6 +100,7 @@ struct Ctx {
   int ntiles = 1;
   int force_T = 0;  // 2-D tile edge set by the batch autotuner (0 = automatic)
   bool nodes_ready = false;
+  unsigned long long gen = 0;  // bumped whenever node set-up rebuilds the node order and work items
   cudaEvent_t ev[7] = {};
   // optional per-call event ring for timing a sequence of device calls
   std::vector<cudaEvent_t> ring;  // 7 events per slot
@@ -222,6 +224,19 @@ static void choose_tiles(Ctx<R> *c)
             g.sx2 = sx;
           }
         }
+    }
+  }
+  // 2-D single precision: column B and B^T on 32^2 tiles, nodes keyed by
+  // (tile, column of CX x-cells by 8 y-cells); not under the batch engine,
+  // which sets its own tiles
+  c->col2 = false;
+  if constexpr (std::is_same<R, float>::value) {
+    const int cx = col2_column_width(g.w);
+    if (g.d == 2 && c->tiled && c->force_T == 0 && T == 32 && cx > 0 && g.n[0] >= 32 && g.n[1] >= 32) {
+      c->col2 = true;
+      g.cs = cx;
+      g.csz = 8;
+      g.sub = (32 / cx) * (32 / 8);
     }
   }
   c->ntiles = 1;
@@ -436,6 +451,7 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
   const long long M = g.M;
   cudaStream_t s = c->stream;
   const bool want_index = (ths->flags & NFFT_SORT_NODES) && ths->index_x && M > 0;
+  ++c->gen;
   if (c->direct && !want_index) {
     c->nodes_ready = true;
     return;
@@ -547,10 +563,23 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   return b;
 }
 
+// the 2-D column B where the plan selected it; false otherwise
+template <typename R>
+static bool b2_stage(Ctx<R> *c, typename Cx<R>::T *f)
+{
+  if constexpr (std::is_same<R, float>::value) {
+    if (!c->col2) return false;
+    launch_b2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
+    return true;
+  }
+  return false;
+}
+
 template <typename R>
 static void b_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
   if (c->group3) launch_b3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, col3_bufs(c), c->stream);
+  else if (b2_stage(c, f)) return;
   else if (c->tiled) launch_b_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_b_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
@@ -565,12 +594,25 @@ static cudaEvent_t *events_for_call(Ctx<R> *c, bool trafo)
   return c->ev;
 }
 
+// the 2-D column B^T where the plan selected it; false otherwise
+template <typename R>
+static bool bt2_stage(Ctx<R> *c, const typename Cx<R>::T *f)
+{
+  if constexpr (std::is_same<R, float>::value) {
+    if (!c->col2) return false;
+    launch_bt2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
+    return true;
+  }
+  return false;
+}
+
 template <typename R>
 static void bt_stage(Ctx<R> *c, const typename Cx<R>::T *f, cudaEvent_t *E)
 {
   GB_CUDA(cudaMemsetAsync(c->grid, 0, (size_t)c->g.n_total * sizeof(typename Cx<R>::T), c->stream));
   GB_CUDA(cudaEventRecord(E[6], c->stream));
   if (c->group3) launch_bt3_group<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, col3_bufs(c), c->stream);
+  else if (bt2_stage(c, f)) return;
   else if (c->tiled) launch_bt_tiled<R>(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
   else launch_bt_generic<R>(c->grid, c->xs, c->perm, f, c->g, c->stream);
 }
@@ -1003,6 +1045,7 @@ extern "C" {
     for (int i = 0; i < 4; ++i) ms4[i] = c->stage_ms[i];                                           \
   }                                                                                                \
   int X##gb_last_launch_count(X##plan *ths) { return ctx_of<R>(ths)->launches; }                  \
+  unsigned long long X##gb_generation(X##plan *ths) { return ctx_of<R>(ths)->gen; }              \
   int X##gb_timing_begin(X##plan *ths, int max_calls) { return timing_begin<R>(ctx_of<R>(ths), max_calls); } \
   int X##gb_timing_end(X##plan *ths, float *sums7, int *counts2)                                    \
   {                                                                                                \

@@ -7,10 +7,11 @@
 // vector2.c:22-74, vector3.c:22-93.
 //
 // When the solver's mv plan is an nfft_plan of this library, the whole
-// iteration stays in HBM: the plan's device f_hat / f buffers stand in for
-// the reference's pointer swaps (solver.c:85-87, 106-108, ...), the step
-// sizes alpha / beta are computed on the device from FP64 inner products (no
-// host round trip inside an iteration), and only the scalars and the
+// iteration stays in HBM: the transforms read and write the solver's device
+// vectors directly in place of the reference's pointer swaps (solver.c:85-87,
+// 106-108, ...), the step sizes alpha / beta are computed on the device from
+// FP64 inner products (no host round trip inside an iteration), a step's
+// launches replay as one CUDA graph, and only the scalars and the
 // user-visible vectors are copied back at the end of each call.  Inner
 // products accumulate in FP64 for both precisions.
 //
@@ -41,6 +42,9 @@ template <> struct SApi<double> {
   static void *dev_x(plan *p) { return nfft_gb_device_x(p); }
   static void trafo_dev(plan *p) { nfft_gb_trafo_device(p); }
   static void adjoint_dev(plan *p) { nfft_gb_adjoint_device(p); }
+  static void trafo_ptr(plan *p, const void *fh, void *f) { nfft_gb_trafo_ptr(p, fh, f); }
+  static void adjoint_ptr(plan *p, const void *f, void *fh) { nfft_gb_adjoint_ptr(p, f, fh); }
+  static unsigned long long gen(plan *p) { return nfft_gb_generation(p); }
 };
 template <> struct SApi<float> {
   typedef solverf_plan_complex splan;
@@ -55,6 +59,9 @@ template <> struct SApi<float> {
   static void *dev_x(plan *p) { return nfftf_gb_device_x(p); }
   static void trafo_dev(plan *p) { nfftf_gb_trafo_device(p); }
   static void adjoint_dev(plan *p) { nfftf_gb_adjoint_device(p); }
+  static void trafo_ptr(plan *p, const void *fh, void *f) { nfftf_gb_trafo_ptr(p, fh, f); }
+  static void adjoint_ptr(plan *p, const void *f, void *fh) { nfftf_gb_adjoint_ptr(p, f, fh); }
+  static unsigned long long gen(plan *p) { return nfftf_gb_generation(p); }
 };
 
 
@@ -145,12 +152,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_partial(const typename Cx<R
   }
 }
 
+// one warp: lane l sums part[l], part[l + 32], ... and a butterfly adds the
+// lanes (a fixed order, so the result does not vary between runs)
 __global__ void k_finish(const double *__restrict__ part, int nblk, double *__restrict__ scal, int op)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
   double s = 0.0;
   if (op != F_ALPHA_CGNE)
-    for (int i = 0; i < nblk; ++i) s += part[i];
+    for (int i = threadIdx.x; i < nblk; i += 32) s += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x != 0) return;
   switch (op) {
     case F_DOT_V_ALPHA:
       scal[S_DOT_V] = s;
@@ -217,6 +229,10 @@ struct SolverState {
   int refresh_every = 0;
   long long iter = 0;
   nfft_plan *plan64 = nullptr;
+  // CUDA graph of one step's launches (steepest descent, CGNR, CGNE)
+  bool use_graph = true;
+  cudaGraphExec_t gexec = nullptr;
+  unsigned long long gen = 0;  // the plan's node set-up it was captured against
 };
 
 static std::mutex g_solver_mu;
@@ -375,6 +391,71 @@ static void dev_before_loop(typename SApi<R>::splan *ths, SolverState<R> *st)
   publish<R>(ths, st, true);
 }
 
+// One steepest-descent, CGNR or CGNE step (solver.c:181-344) on the
+// solver's stream.  The transforms run straight on the solver's device
+// vectors (the plan's own buffers only take the weighted copies), and every
+// scalar stays on the device, so the sequence has no host dependency and can
+// be captured as a graph.
+template <typename R>
+static void enqueue_step(SolverState<R> *st, bool refresh)
+{
+  typedef typename Cx<R>::T C;
+  const long long M = st->M, N = st->N;
+  const unsigned fl = st->flags;
+  const R *w = (fl & PRECOMPUTE_WEIGHT) ? st->w : nullptr;
+  const R *wh = (fl & PRECOMPUTE_DAMP) ? st->wh : nullptr;
+  // out = A (wh .* in)
+  auto trafo_w = [&](const C *in, C *out) {
+    if (wh) {
+      wcopy<R>(st, st->mv_fh, in, wh, N);
+      in = st->mv_fh;
+    }
+    SApi<R>::trafo_ptr(st->plan, in, out);
+  };
+  // out = A^H (w .* in)
+  auto adjoint_w = [&](const C *in, C *out) {
+    if (w) {
+      wcopy<R>(st, st->mv_f, in, w, M);
+      in = st->mv_f;
+    }
+    SApi<R>::adjoint_ptr(st->plan, in, out);
+  };
+  if (fl & STEEPEST_DESCENT) {
+    // solver.c:181-229
+    trafo_w(st->z, st->v);
+    dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
+    upd<R>(st, st->fh, st->z, wh, N, S_ALPHA, 1.0);
+    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+    if (refresh) refresh_residual<R>(st);
+    dot_into<R>(st, st->r, w, M, F_DOT_R);
+    adjoint_w(st->r, st->z);
+    dot_into<R>(st, st->z, wh, N, F_DOT_Z);
+  } else if (fl & CGNR) {
+    // solver.c:232-292
+    trafo_w(st->p, st->v);
+    dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
+    upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
+    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+    if (refresh) refresh_residual<R>(st);
+    dot_into<R>(st, st->r, w, M, F_DOT_R);
+    adjoint_w(st->r, st->z);
+    dot_into<R>(st, st->z, wh, N, F_DOT_Z_BETA);
+    axpy<R>(st, st->p, st->z, N, S_BETA);
+  } else if (fl & CGNE) {
+    // solver.c:295-344
+    k_finish<<<1, 32, 0, st->s>>>(st->part, 0, st->scal, F_ALPHA_CGNE);
+    GB_LAUNCHED("finish");
+    upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
+    trafo_w(st->p, st->v);
+    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+    if (refresh) refresh_residual<R>(st);
+    dot_into<R>(st, st->r, w, M, F_DOT_R_BETA);
+    adjoint_w(st->r, st->mv_fh);
+    axpy<R>(st, st->p, st->mv_fh, N, S_BETA);
+    dot_into<R>(st, st->p, wh, N, F_DOT_P);
+  }
+}
+
 template <typename R>
 static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
 {
@@ -386,7 +467,7 @@ static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
   ++st->iter;
   const bool refresh = st->refresh_every > 0 && (st->iter % st->refresh_every) == 0;
   if (fl & LANDWEBER) {
-    // solver.c:128-178
+    // solver.c:128-178; the step size comes from the caller every step
     double a = (double)ths->alpha_iter;
     GB_CUDA(cudaMemcpyAsync(st->scal + S_ALPHA, &a, sizeof(double), cudaMemcpyHostToDevice, st->s));
     upd<R>(st, st->fh, st->z, wh, N, S_ALPHA, 1.0);
@@ -400,49 +481,24 @@ static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
     SApi<R>::adjoint_dev(st->plan);
     dcopy<R>(st, st->z, st->mv_fh, N * sizeof(C), cudaMemcpyDeviceToDevice);
     if (fl & NORMS_FOR_LANDWEBER) dot_into<R>(st, st->z, wh, N, F_DOT_Z);
-  } else if (fl & STEEPEST_DESCENT) {
-    // solver.c:181-229
-    wcopy<R>(st, st->mv_fh, st->z, wh, N);
-    SApi<R>::trafo_dev(st->plan);
-    dcopy<R>(st, st->v, st->mv_f, M * sizeof(C), cudaMemcpyDeviceToDevice);
-    dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
-    upd<R>(st, st->fh, st->z, wh, N, S_ALPHA, 1.0);
-    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R);
-    wcopy<R>(st, st->mv_f, st->r, w, M);
-    SApi<R>::adjoint_dev(st->plan);
-    dcopy<R>(st, st->z, st->mv_fh, N * sizeof(C), cudaMemcpyDeviceToDevice);
-    dot_into<R>(st, st->z, wh, N, F_DOT_Z);
-  } else if (fl & CGNR) {
-    // solver.c:232-292
-    wcopy<R>(st, st->mv_fh, st->p, wh, N);
-    SApi<R>::trafo_dev(st->plan);
-    dcopy<R>(st, st->v, st->mv_f, M * sizeof(C), cudaMemcpyDeviceToDevice);
-    dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
-    upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
-    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R);
-    wcopy<R>(st, st->mv_f, st->r, w, M);
-    SApi<R>::adjoint_dev(st->plan);
-    dcopy<R>(st, st->z, st->mv_fh, N * sizeof(C), cudaMemcpyDeviceToDevice);
-    dot_into<R>(st, st->z, wh, N, F_DOT_Z_BETA);
-    axpy<R>(st, st->p, st->z, N, S_BETA);
-  } else if (fl & CGNE) {
-    // solver.c:295-344
-    k_finish<<<1, 32, 0, st->s>>>(st->part, 0, st->scal, F_ALPHA_CGNE);
-    GB_LAUNCHED("finish");
-    upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
-    wcopy<R>(st, st->mv_fh, st->p, wh, N);
-    SApi<R>::trafo_dev(st->plan);
-    upd<R>(st, st->r, st->mv_f, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R_BETA);
-    wcopy<R>(st, st->mv_f, st->r, w, M);
-    SApi<R>::adjoint_dev(st->plan);
-    axpy<R>(st, st->p, st->mv_fh, N, S_BETA);
-    dot_into<R>(st, st->p, wh, N, F_DOT_P);
+  } else if (st->use_graph && !refresh) {
+    const unsigned long long gen = SApi<R>::gen(st->plan);
+    if (!st->gexec || st->gen != gen) {
+      if (st->gexec) {
+        GB_CUDA(cudaGraphExecDestroy(st->gexec));
+        st->gexec = nullptr;
+      }
+      cudaGraph_t gph = nullptr;
+      GB_CUDA(cudaStreamBeginCapture(st->s, cudaStreamCaptureModeRelaxed));
+      enqueue_step<R>(st, false);
+      GB_CUDA(cudaStreamEndCapture(st->s, &gph));
+      GB_CUDA(cudaGraphInstantiate(&st->gexec, gph, 0));
+      GB_CUDA(cudaGraphDestroy(gph));
+      st->gen = gen;
+    }
+    GB_CUDA(cudaGraphLaunch(st->gexec, st->s));
+  } else {
+    enqueue_step<R>(st, refresh);
   }
   publish<R>(ths, st, false);
 }
@@ -631,6 +687,7 @@ static void finalize_solver(typename SApi<R>::splan *ths)
   SolverState<R> *st = state_of<R>(ths);
   if (st) {
     cudaStreamSynchronize(st->s);
+    if (st->gexec) cudaGraphExecDestroy(st->gexec);
     cudaFree(st->y);
     cudaFree(st->r);
     cudaFree(st->v);
@@ -722,6 +779,13 @@ extern "C" {
   {                                                                                             \
     SolverState<R> *st = state_of<R>(ths);                                                      \
     return st ? (void *)st->y : nullptr;                                                        \
+  }                                                                                             \
+  int X##gb_set_graphs(X##plan_complex *ths, int on)                                            \
+  {                                                                                             \
+    SolverState<R> *st = state_of<R>(ths);                                                      \
+    if (!st) return -1;                                                                         \
+    st->use_graph = on != 0;                                                                    \
+    return 0;                                                                                   \
   }
 
 GB_SOLVER_API(solver_, double)

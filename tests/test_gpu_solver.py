@@ -128,3 +128,56 @@ def test_single_precision_refresh_converges(gpulib):
     s.finalize()
     p.finalize()
     assert err < 1e-3, err
+
+
+def _set_graphs(lib, s, single, on):
+    import ctypes
+    fn = getattr(lib, ("solverf_" if single else "solver_") + "gb_set_graphs")
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    fn.restype = ctypes.c_int
+    assert fn(ctypes.addressof(s.s), int(on)) == 0
+
+
+@pytest.mark.parametrize("single", [False, True])
+@pytest.mark.parametrize("flags", [abi.CGNR | abi.PRECOMPUTE_WEIGHT | abi.PRECOMPUTE_DAMP, abi.CGNE,
+                                   abi.STEEPEST_DESCENT | abi.PRECOMPUTE_WEIGHT])
+def test_graph_steps_match_launched_steps(gpulib, single, flags):
+    """Steps replayed from the captured CUDA graph give the iterates and
+    scalars of the same steps launched one by one, also across a change of
+    the nodes (precompute_one_psi again), which re-captures the graph.  The
+    adjoint's atomic accumulation orders its additions differently from run
+    to run, so two runs agree to rounding, not bit for bit."""
+    N, M, m = [32, 32], 2500, 6
+    x, _, y = seeded_case(N, M, seed=21)
+    x2, _, _ = seeded_case(N, M, seed=22)
+    rng = np.random.default_rng(4)
+    w = rng.uniform(0.5, 1.5, M)
+    wh = rng.uniform(0.5, 1.5, 1024)
+    dt = np.float32 if single else np.float64
+    runs = []
+    for graphs in (True, False):
+        p = gpu_plan(gpulib, single, N, M, m, x.astype(dt))
+        s = Solver(p, flags)
+        _set_graphs(gpulib, s, single, graphs)
+        s.y[:] = y
+        if flags & abi.PRECOMPUTE_WEIGHT:
+            s.w[:] = w
+        if flags & abi.PRECOMPUTE_DAMP:
+            s.w_hat[:] = wh
+        s.f_hat_iter[:] = 0
+        s.before_loop()
+        out = []
+        for it in range(6):
+            if it == 3:
+                p.x[:] = x2.astype(dt)
+                p.precompute_one_psi()
+            s.loop_one_step()
+            out.append((s.f_hat_iter.copy(), tuple(s.scalars().values())))
+        s.finalize()
+        p.finalize()
+        runs.append(out)
+    tol = 1e-4 if single else 1e-11
+    for it, ((fa, sa), (fb, sb)) in enumerate(zip(*runs)):
+        assert rel_l2(fa, fb) < tol, (it, rel_l2(fa, fb))
+        for a, b in zip(sa, sb):
+            assert abs(a - b) <= 10 * tol * abs(b) + 1e-30, (it, a, b)

@@ -1,4 +1,4 @@
-"""The polynomial window of the single-precision 3-D kernels, checked on the
+"""The polynomial window of the single-precision 2-D and 3-D kernels, checked on the
 CPU against the Kaiser-Bessel window of the reference (include/infft.h:209-222):
 phi(t) = sinh(b sqrt(m^2 - t^2)) / (pi sqrt(m^2 - t^2)) inside the support,
 sin(b sqrt(t^2 - m^2)) / (pi sqrt(t^2 - m^2)) outside, b / pi on its edge,
@@ -33,7 +33,8 @@ def horner_f32(c, s):
     return v.astype(np.float64)
 
 
-@pytest.mark.parametrize("m,sigma", [(2, 2.0), (3, 2.0), (4, 2.0), (4, 1.5), (4, 1.25), (3, 1.25)])
+@pytest.mark.parametrize("m,sigma", [(2, 2.0), (3, 2.0), (4, 2.0), (4, 1.5), (4, 1.25), (3, 1.25), (5, 2.0), (6, 2.0),
+                                     (7, 2.0), (6, 1.5)])
 def test_polynomial_window_matches_kaiser_bessel(m, sigma):
     lib = nfft_gb300.lib()
     fit = lib.nfft_gb_kb_poly_fit

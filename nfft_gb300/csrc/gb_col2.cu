@@ -343,6 +343,144 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_b2_col(const WorkItem *__rest
   }
 }
 
+// ---------------------------------------------------------------- double
+// The B^T above in double precision (the FP64 transforms of the
+// mixed-precision solver and of double plans): the same columns and lane
+// roles, FP64 accumulators (one FMA per y position and component), the
+// window evaluated exactly per node, four warps per CTA for the larger
+// vectors.
+static constexpr int C2D_THREADS = 128;
+static constexpr int C2D_WARPS = C2D_THREADS / 32;
+
+template <int W>
+struct C2D {
+  typedef C2<W> P;
+  static constexpr int NP = 2 * P::HP;       // y positions per half-warp
+  static constexpr int XS = 17;              // x vector stride (complex)
+  static constexpr int YS = 2 * NP + 2;      // y vector stride (doubles; even: 16-byte pairs)
+  static constexpr int WARP_DOUBLES = 2 * XS * C2_CHUNK + YS * C2_CHUNK;
+};
+
+template <int W>
+static size_t c2d_smem_bytes()
+{
+  typedef C2<W> P;
+  return (size_t)C2D_WARPS * C2D<W>::WARP_DOUBLES * sizeof(double) + (size_t)P::EXT * P::SY * sizeof(double2);
+}
+
+template <int W>
+__global__ void __launch_bounds__(C2D_THREADS) k_bt2_col_d(const WorkItem *__restrict__ items,
+                                                           double2 *__restrict__ grid,
+                                                           const double *__restrict__ xs,
+                                                           const uint32_t *__restrict__ perm,
+                                                           const double2 *__restrict__ f, Geom<double> g)
+{
+  typedef C2<W> P;
+  typedef C2D<W> Q;
+  constexpr int CX = P::CX, NP = Q::NP, SY = P::SY;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *const base = reinterpret_cast<double *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double2 *const wx = reinterpret_cast<double2 *>(base + warp * Q::WARP_DOUBLES);  // stride XS
+  double *const wy = base + warp * Q::WARP_DOUBLES + 2 * Q::XS * C2_CHUNK;           // stride YS
+  double2 *const sg = reinterpret_cast<double2 *>(base + C2D_WARPS * Q::WARP_DOUBLES);
+
+  const WorkItem it = items[blockIdx.x];
+  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  for (int i = threadIdx.x; i < P::EXT * SY; i += C2D_THREADS) sg[i] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const int h = lane >> 4, r = lane & 15;
+
+  for (int a = it.start + warp * C2_CHUNK; a < it.end; a += C2D_WARPS * C2_CHUNK) {
+    const int np = min(C2_CHUNK, it.end - a);
+    int col = -1;
+    if (lane < np) {
+      const int i = a + lane;
+      const double x0 = xs[2LL * i], x1 = xs[2LL * i + 1];
+      const int u0 = node_u<double>(x0, g.nR[0], g.m), u1 = node_u<double>(x1, g.nR[1], g.m);
+      const int ux = min(max(wrap(u0, g.n[0]) - org0, 0), C2_TILE - 1);
+      const int uy = min(max(wrap(u1, g.n[1]) - org1, 0), C2_TILE - 1);
+      const int ox = ux % CX, oy = uy % C2_CY;
+      col = (ux / CX) * C2_SLABS + uy / C2_CY;
+      const double2 fj = f[perm[i]];
+      double v[W];
+      double2 *xv = wx + Q::XS * lane;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) xv[q] = make_double2(0.0, 0.0);
+      node_psi<double, W>(x0, u0, g.nR[0], g.mm, g.b[0], v);
+#pragma unroll
+      for (int l = 0; l < W; ++l) xv[ox + l] = make_double2(v[l] * fj.x, v[l] * fj.y);
+      double *yv = wy + Q::YS * lane;
+#pragma unroll
+      for (int q = 0; q < 2 * NP; ++q) yv[q] = 0.0;
+      node_psi<double, W>(x1, u1, g.nR[1], g.mm, g.b[1], v);
+#pragma unroll
+      for (int l = 0; l < W; ++l) yv[oy + l] = v[l];
+    }
+    const int prevc = __shfl_up_sync(0xffffffffu, col, 1);
+    unsigned starts = __ballot_sync(0xffffffffu, lane < np && (lane == 0 || col != prevc));
+    __syncwarp();
+    while (starts) {
+      const int s = __ffs(starts) - 1;
+      starts &= starts - 1;
+      const int e = starts ? __ffs(starts) - 1 : np;
+      const int c = __shfl_sync(0xffffffffu, col, s);
+      double ar[NP], ai[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) ar[q] = ai[q] = 0.0;
+      for (int j = s; j < e; ++j) {
+        const double2 xf = wx[Q::XS * j + r];
+        const double2 *yp = reinterpret_cast<const double2 *>(wy + Q::YS * j + h * NP);
+#pragma unroll
+        for (int q = 0; q < NP / 2; ++q) {
+          const double2 w = yp[q];
+          ar[2 * q] = fma(w.x, xf.x, ar[2 * q]);
+          ai[2 * q] = fma(w.x, xf.y, ai[2 * q]);
+          ar[2 * q + 1] = fma(w.y, xf.x, ar[2 * q + 1]);
+          ai[2 * q + 1] = fma(w.y, xf.y, ai[2 * q + 1]);
+        }
+      }
+      const int xc = c / C2_SLABS, sl = c - xc * C2_SLABS;
+      if (r < P::ROWS) {
+        double2 *p = sg + (CX * xc + r) * SY + C2_CY * sl + h * NP;
+        const int nv = P::NPOS - h * NP;
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+          if (q < nv && (ar[q] != 0.0 || ai[q] != 0.0)) {
+            atomicAdd(&p[q].x, ar[q]);
+            atomicAdd(&p[q].y, ai[q]);
+          }
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < P::EXT * P::EXT; idx += C2D_THREADS) {
+    const int rx = idx / P::EXT, ry = idx - rx * P::EXT;
+    const double2 v = sg[rx * SY + ry];
+    if (v.x != 0.0 || v.y != 0.0) {
+      int p0 = org0 + rx, p1 = org1 + ry;
+      while (p0 >= g.n[0]) p0 -= g.n[0];
+      while (p1 >= g.n[1]) p1 -= g.n[1];
+      global_add_c(grid + (long long)p0 * g.n[1] + p1, v);
+    }
+  }
+}
+
+template <int W>
+static void run_bt2_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
+                      const double2 *f, const Geom<double> &g, cudaStream_t s)
+{
+  static bool attr = false;
+  const size_t smem = c2d_smem_bytes<W>();
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(k_bt2_col_d<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  k_bt2_col_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
+  GB_LAUNCHED("bt2_col_d");
+}
+
 template <int W>
 static void run_col2(bool adjoint, const WorkItem *items, int nitems, float2 *grid, const float *xs,
                      const uint32_t *perm, float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
@@ -408,6 +546,26 @@ void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const 
                    float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
   launch_col2(false, items, nitems, const_cast<float2 *>(grid), xs, perm, f, g, poly, s);
+}
+
+}  // namespace gb
+
+namespace gb {
+
+void launch_bt2_col_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
+                      const double2 *f, const Geom<double> &g, cudaStream_t s)
+{
+  if (nitems <= 0) return;
+  switch (g.w) {
+#define GB_C2D_RUN(W)                                         \
+  case W:                                                     \
+    run_bt2_d<W>(items, nitems, grid, xs, perm, f, g, s); \
+    return;
+    GB_COL2_WIDTHS(GB_C2D_RUN)
+#undef GB_C2D_RUN
+    default:
+      fatal("no 2-D column kernel for w=%d", g.w);
+  }
 }
 
 }  // namespace gb

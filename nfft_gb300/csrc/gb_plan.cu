@@ -71,7 +71,7 @@ struct Ctx {
   bool tiled = false;
   bool group3 = false;  // 3-D sub-cell group kernels
   WinPoly poly = {};     // polynomial window of the single-precision 2-D / 3-D kernels
-  bool col2 = false;     // single-precision 2-D column B and B^T (nodes keyed by column)
+  bool col2 = false;     // 2-D column B^T (and B in single precision); nodes keyed by column
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
@@ -126,6 +126,17 @@ static int ceil_log2(long long v)
   int b = 0;
   while ((1LL << b) < v) ++b;
   return b;
+}
+
+// Nodes per work item of the transform kernels: the 3-D group kernels take
+// large items; 2-D double precision, bound by FP64 arithmetic, takes small
+// ones so that crowded tiles spread over many SMs.
+template <typename R>
+static int item_chunk(const Ctx<R> *c)
+{
+  if (c->group3) return group3_max_item();
+  if (std::is_same<R, double>::value && c->g.d == 2) return 128;
+  return 1024;
 }
 
 // Tile edge per dimension for the shared-memory kernels: the largest
@@ -226,11 +237,11 @@ static void choose_tiles(Ctx<R> *c)
         }
     }
   }
-  // 2-D single precision: column B and B^T on 32^2 tiles, nodes keyed by
+  // 2-D: column B^T (and B in single precision) on 32^2 tiles, nodes keyed by
   // (tile, column of CX x-cells by 8 y-cells); not under the batch engine,
   // which sets its own tiles
   c->col2 = false;
-  if constexpr (std::is_same<R, float>::value) {
+  {
     const int cx = col2_column_width(g.w);
     if (g.d == 2 && c->tiled && c->force_T == 0 && T == 32 && cx > 0 && g.n[0] >= 32 && g.n[1] >= 32) {
       c->col2 = true;
@@ -413,7 +424,7 @@ static void init_help(typename Api<R>::plan *ths)
     dev_alloc<R>((void **)&c->xs, M * d * sizeof(R));
     dev_alloc<R>((void **)&c->perm, M * sizeof(uint32_t));
     dev_alloc<R>((void **)&c->tile_start, ((size_t)c->ntiles + 1) * sizeof(uint32_t));
-    const int chunk = 1024;
+    const int chunk = std::min(item_chunk(c), 1024);  // the item buffers hold any chunk >= this
     dev_alloc<R>((void **)&c->items, ((size_t)c->ntiles + M / chunk + 2) * sizeof(WorkItem));
     c->col3 = c->group3 && sizeof(R) == 4 && group3_column_supported<R>(g.w);
     if (c->col3) {
@@ -499,7 +510,7 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
       dev_alloc<R>((void **)&cnt, (size_t)c->ntiles * 4);
       dev_alloc<R>((void **)&off, (size_t)c->ntiles * 4);
     }
-    const int chunk = c->group3 ? group3_max_item() : 1024;
+    const int chunk = item_chunk(c);
     c->nitems = c->tiled ? build_work_items(c->tile_start, c->ntiles, chunk, c->items, cnt, off,
                                             total, temp, s)
                          : 0;
@@ -563,7 +574,9 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   return b;
 }
 
-// the 2-D column B where the plan selected it; false otherwise
+// the 2-D column B where the plan selected it (single precision; double
+// keeps the per-node gather, whose FP64 arithmetic is the smaller); false
+// otherwise
 template <typename R>
 static bool b2_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
@@ -598,12 +611,12 @@ static cudaEvent_t *events_for_call(Ctx<R> *c, bool trafo)
 template <typename R>
 static bool bt2_stage(Ctx<R> *c, const typename Cx<R>::T *f)
 {
-  if constexpr (std::is_same<R, float>::value) {
-    if (!c->col2) return false;
+  if (!c->col2) return false;
+  if constexpr (std::is_same<R, float>::value)
     launch_bt2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
-    return true;
-  }
-  return false;
+  else
+    launch_bt2_col_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+  return true;
 }
 
 template <typename R>
@@ -1092,7 +1105,7 @@ void plan_retile_f(void *pp, int T)
   GB_CUDA(cudaFree(c->items));
   const size_t M = (size_t)std::max<long long>(c->g.M, 1);
   dev_alloc<float>((void **)&c->tile_start, ((size_t)c->ntiles + 1) * sizeof(uint32_t));
-  dev_alloc<float>((void **)&c->items, ((size_t)c->ntiles + M / 1024 + 2) * sizeof(WorkItem));
+  dev_alloc<float>((void **)&c->items, ((size_t)c->ntiles + M / std::min(item_chunk(c), 1024) + 2) * sizeof(WorkItem));
   nodes_from_device<float>(p, c);
 }
 

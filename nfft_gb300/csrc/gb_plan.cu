@@ -129,13 +129,14 @@ static int ceil_log2(long long v)
 }
 
 // Nodes per work item of the transform kernels: the 3-D group kernels take
-// large items; 2-D double precision, bound by FP64 arithmetic, takes small
-// ones so that crowded tiles spread over many SMs.
+// large items; 2-D plans take small ones so that crowded tiles spread over
+// many SMs (double precision, bound by FP64 arithmetic, the smallest).
 template <typename R>
 static int item_chunk(const Ctx<R> *c)
 {
   if (c->group3) return group3_max_item();
   if (std::is_same<R, double>::value && c->g.d == 2) return 128;
+  if (c->col2) return 256;  // 2-D column kernels: eight warp tasks of 32 nodes
   return 1024;
 }
 

@@ -128,41 +128,9 @@ __global__ void k_axpy(typename Cx<R>::T *__restrict__ x, const typename Cx<R>::
   }
 }
 
-// per-block partial sums of w |x|^2 in FP64
-template <typename R>
-__global__ void __launch_bounds__(RED_THREADS) k_dot_partial(const typename Cx<R>::T *__restrict__ x,
-                                                             const R *__restrict__ w, long long n,
-                                                             double *__restrict__ part)
+// The scalar update that ends a reduction (s = the reduced value).
+__device__ __forceinline__ void finish_op(double s, double *__restrict__ scal, int op)
 {
-  __shared__ double sm[RED_THREADS / 32];
-  double s = 0.0;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    const typename Cx<R>::T v = x[k];
-    const double a = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-    s += w ? (double)w[k] * a : a;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int i = 0; i < RED_THREADS / 32; ++i) t += sm[i];
-    part[blockIdx.x] = t;
-  }
-}
-
-// one warp: lane l sums part[l], part[l + 32], ... and a butterfly adds the
-// lanes (a fixed order, so the result does not vary between runs)
-__global__ void k_finish(const double *__restrict__ part, int nblk, double *__restrict__ scal, int op)
-{
-  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
-  double s = 0.0;
-  if (op != F_ALPHA_CGNE)
-    for (int i = threadIdx.x; i < nblk; i += 32) s += part[i];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (threadIdx.x != 0) return;
   switch (op) {
     case F_DOT_V_ALPHA:
       scal[S_DOT_V] = s;
@@ -191,6 +159,107 @@ __global__ void k_finish(const double *__restrict__ part, int nblk, double *__re
       scal[S_ALPHA] = scal[S_DOT_R] / scal[S_DOT_P];
       break;
   }
+}
+
+// one warp: lane l sums part[l], part[l + 32], ... and a butterfly adds the
+// lanes (a fixed order, so the result does not vary between runs)
+__device__ __forceinline__ double sum_parts(const volatile double *part, int nblk)
+{
+  double s = 0.0;
+  for (int i = threadIdx.x & 31; i < nblk; i += 32) s += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+__global__ void k_finish(const double *__restrict__ part, int nblk, double *__restrict__ scal, int op)
+{
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const double s = op != F_ALPHA_CGNE ? sum_parts(part, nblk) : 0.0;
+  if (threadIdx.x == 0) finish_op(s, scal, op);
+}
+
+// Block sum of the threads' values v into part[blockIdx.x]; the block that
+// finishes last (ticket) then adds the blocks' sums in a fixed order,
+// applies the scalar update and resets the ticket for the next reduction.
+__device__ __forceinline__ void reduce_and_finish(double v, double *__restrict__ part, unsigned *__restrict__ ticket,
+                                                  double *__restrict__ scal, int op)
+{
+  __shared__ double sm[RED_THREADS / 32];
+  __shared__ bool last;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < RED_THREADS / 32; ++i) t += sm[i];
+    part[blockIdx.x] = t;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x < 32) {
+    __threadfence();
+    const double s = sum_parts(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      finish_op(s, scal, op);
+      *ticket = 0;
+    }
+  }
+}
+
+// sum of w |x|^2 (w == nullptr: |x|^2) and its scalar update, one launch
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) k_dot(const typename Cx<R>::T *__restrict__ x,
+                                                     const R *__restrict__ w, long long n,
+                                                     double *__restrict__ part, unsigned *__restrict__ ticket,
+                                                     double *__restrict__ scal, int op)
+{
+  double s = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const typename Cx<R>::T v = x[k];
+    const double a = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    s += w ? (double)w[k] * a : a;
+  }
+  reduce_and_finish(s, part, ticket, scal, op);
+}
+
+// f_hat += alpha wh .* p (N values, skipped when p == nullptr) and
+// r -= alpha v (M values), then the sum of w |r|^2 and its scalar update
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) k_upd_dot(typename Cx<R>::T *__restrict__ fh,
+                                                         const typename Cx<R>::T *__restrict__ p,
+                                                         const R *__restrict__ wh, long long N,
+                                                         typename Cx<R>::T *__restrict__ r,
+                                                         const typename Cx<R>::T *__restrict__ v,
+                                                         const R *__restrict__ w, long long M,
+                                                         double *__restrict__ part, unsigned *__restrict__ ticket,
+                                                         double *__restrict__ scal, int op)
+{
+  const double a = scal[S_ALPHA];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p)
+    for (long long k = k0; k < N; k += stride) {
+      const double c = wh ? a * (double)wh[k] : a;
+      typename Cx<R>::T u = fh[k];
+      const typename Cx<R>::T d = p[k];
+      u.x = (R)((double)u.x + c * (double)d.x);
+      u.y = (R)((double)u.y + c * (double)d.y);
+      fh[k] = u;
+    }
+  double s = 0.0;
+  for (long long k = k0; k < M; k += stride) {
+    typename Cx<R>::T u = r[k];
+    const typename Cx<R>::T d = v[k];
+    u.x = (R)((double)u.x - a * (double)d.x);
+    u.y = (R)((double)u.y - a * (double)d.y);
+    r[k] = u;
+    const double q = (double)u.x * (double)u.x + (double)u.y * (double)u.y;
+    s += w ? (double)w[k] * q : q;
+  }
+  reduce_and_finish(s, part, ticket, scal, op);
 }
 
 // FP64 residual refresh helpers: r = y - A f (A f in FP64), cast to plan precision
@@ -223,6 +292,7 @@ struct SolverState {
   R *w = nullptr, *wh = nullptr;
   C *mv_f = nullptr, *mv_fh = nullptr;  // the plan's device f / f_hat
   double *scal = nullptr, *part = nullptr;
+  unsigned *ticket = nullptr;  // blocks done in the current reduction (zero between launches)
   double *scal_host = nullptr;
   int sync_level = 2;
   // FP64 residual refresh (single-precision solvers)
@@ -257,10 +327,19 @@ static unsigned grid_for(long long n)
 template <typename R>
 static void dot_into(SolverState<R> *st, const typename Cx<R>::T *x, const R *w, long long n, int op)
 {
-  k_dot_partial<R><<<RED_BLOCKS, RED_THREADS, 0, st->s>>>(x, w, n, st->part);
-  GB_LAUNCHED("dot_partial");
-  k_finish<<<1, 32, 0, st->s>>>(st->part, RED_BLOCKS, st->scal, op);
-  GB_LAUNCHED("finish");
+  k_dot<R><<<RED_BLOCKS, RED_THREADS, 0, st->s>>>(x, w, n, st->part, st->ticket, st->scal, op);
+  GB_LAUNCHED("dot");
+}
+
+// fh += alpha wh .* p (p == nullptr: no update), r -= alpha v, then the
+// reduction of w |r|^2 into op
+template <typename R>
+static void upd_dot(SolverState<R> *st, typename Cx<R>::T *fh, const typename Cx<R>::T *p, const R *wh,
+                    typename Cx<R>::T *r, const typename Cx<R>::T *v, const R *w, int op)
+{
+  k_upd_dot<R><<<RED_BLOCKS, RED_THREADS, 0, st->s>>>(fh, p, wh, st->N, r, v, w, st->M, st->part, st->ticket,
+                                                      st->scal, op);
+  GB_LAUNCHED("upd_dot");
 }
 
 template <typename R>
@@ -424,20 +503,28 @@ static void enqueue_step(SolverState<R> *st, bool refresh)
     // solver.c:181-229
     trafo_w(st->z, st->v);
     dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
-    upd<R>(st, st->fh, st->z, wh, N, S_ALPHA, 1.0);
-    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R);
+    if (refresh) {
+      upd<R>(st, st->fh, st->z, wh, N, S_ALPHA, 1.0);
+      upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+      refresh_residual<R>(st);
+      dot_into<R>(st, st->r, w, M, F_DOT_R);
+    } else {
+      upd_dot<R>(st, st->fh, st->z, wh, st->r, st->v, w, F_DOT_R);
+    }
     adjoint_w(st->r, st->z);
     dot_into<R>(st, st->z, wh, N, F_DOT_Z);
   } else if (fl & CGNR) {
     // solver.c:232-292
     trafo_w(st->p, st->v);
     dot_into<R>(st, st->v, w, M, F_DOT_V_ALPHA);
-    upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
-    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R);
+    if (refresh) {
+      upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
+      upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+      refresh_residual<R>(st);
+      dot_into<R>(st, st->r, w, M, F_DOT_R);
+    } else {
+      upd_dot<R>(st, st->fh, st->p, wh, st->r, st->v, w, F_DOT_R);
+    }
     adjoint_w(st->r, st->z);
     dot_into<R>(st, st->z, wh, N, F_DOT_Z_BETA);
     axpy<R>(st, st->p, st->z, N, S_BETA);
@@ -447,9 +534,13 @@ static void enqueue_step(SolverState<R> *st, bool refresh)
     GB_LAUNCHED("finish");
     upd<R>(st, st->fh, st->p, wh, N, S_ALPHA, 1.0);
     trafo_w(st->p, st->v);
-    upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
-    if (refresh) refresh_residual<R>(st);
-    dot_into<R>(st, st->r, w, M, F_DOT_R_BETA);
+    if (refresh) {
+      upd<R>(st, st->r, st->v, nullptr, M, S_ALPHA, -1.0);
+      refresh_residual<R>(st);
+      dot_into<R>(st, st->r, w, M, F_DOT_R_BETA);
+    } else {
+      upd_dot<R>(st, st->fh, nullptr, wh, st->r, st->v, w, F_DOT_R_BETA);
+    }
     adjoint_w(st->r, st->mv_fh);
     axpy<R>(st, st->p, st->mv_fh, N, S_BETA);
     dot_into<R>(st, st->p, wh, N, F_DOT_P);
@@ -674,6 +765,8 @@ static void init_advanced(typename SApi<R>::splan *ths, typename SApi<R>::mvplan
   GB_CUDA(cudaMalloc(&st->wh, Nz * sizeof(R)));
   GB_CUDA(cudaMalloc(&st->scal, S_COUNT * sizeof(double)));
   GB_CUDA(cudaMalloc(&st->part, RED_BLOCKS * sizeof(double)));
+  GB_CUDA(cudaMalloc(&st->ticket, sizeof(unsigned)));
+  GB_CUDA(cudaMemset(st->ticket, 0, sizeof(unsigned)));
   GB_CUDA(cudaMallocHost(&st->scal_host, S_COUNT * sizeof(double)));
   st->mv_f = (C *)SApi<R>::dev_f(st->plan);
   st->mv_fh = (C *)SApi<R>::dev_fhat(st->plan);
@@ -698,6 +791,7 @@ static void finalize_solver(typename SApi<R>::splan *ths)
     cudaFree(st->wh);
     cudaFree(st->scal);
     cudaFree(st->part);
+    cudaFree(st->ticket);
     cudaFreeHost(st->scal_host);
     if (st->plan64) {
       nfft_finalize(st->plan64);

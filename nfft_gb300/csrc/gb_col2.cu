@@ -1,5 +1,6 @@
-// gb_col2.cu -- single-precision 2-D B^T (adjoint spreading) and B
-// (interpolation) by x-row strips of sub-cell columns.
+// gb_col2.cu -- 2-D B^T (adjoint spreading, single and double precision)
+// and B (interpolation, single precision) by x-row strips of sub-cell
+// columns.
 //
 // B^T: reference nfft_adjoint_2d_B (nfft.c:3583-3805) with its blockwise
 // scatter (nfft.c:3064-3139): g[l mod n] += phi_0 phi_1 f_j over the
@@ -482,26 +483,31 @@ static void run_bt2_d(const WorkItem *items, int nitems, double2 *grid, const do
 }
 
 template <int W>
-static void run_col2(bool adjoint, const WorkItem *items, int nitems, float2 *grid, const float *xs,
-                     const uint32_t *perm, float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+static void run_bt2(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
-  static bool attr_t = false, attr_b = false;
-  const size_t smem = c2_smem_bytes<W>(adjoint);
-  if (adjoint) {
-    if (!attr_t) {
-      GB_CUDA(cudaFuncSetAttribute(k_bt2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      attr_t = true;
-    }
-    k_bt2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
-    GB_LAUNCHED("bt2_col");
-  } else {
-    if (!attr_b) {
-      GB_CUDA(cudaFuncSetAttribute(k_b2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      attr_b = true;
-    }
-    k_b2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
-    GB_LAUNCHED("b2_col");
+  static bool attr = false;
+  const size_t smem = c2_smem_bytes<W>(true);
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(k_bt2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
   }
+  k_bt2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
+  GB_LAUNCHED("bt2_col");
+}
+
+template <int W>
+static void run_b2(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
+                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+{
+  static bool attr = false;
+  const size_t smem = c2_smem_bytes<W>(false);
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(k_b2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  k_b2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
+  GB_LAUNCHED("b2_col");
 }
 
 #define GB_COL2_WIDTHS(X) X(6) X(8) X(10) X(12) X(14) X(16)
@@ -519,15 +525,14 @@ int col2_column_width(int w)
   }
 }
 
-static void launch_col2(bool adjoint, const WorkItem *items, int nitems, float2 *grid, const float *xs,
-                        const uint32_t *perm, float2 *f, const Geom<float> &g, const WinPoly &poly,
-                        cudaStream_t s)
+void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
   if (nitems <= 0) return;
   switch (g.w) {
-#define GB_C2_RUN(W)                                                            \
-  case W:                                                                       \
-    run_col2<W>(adjoint, items, nitems, grid, xs, perm, f, g, poly, s); \
+#define GB_C2_RUN(W)                                                 \
+  case W:                                                            \
+    run_bt2<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
     return;
     GB_COL2_WIDTHS(GB_C2_RUN)
 #undef GB_C2_RUN
@@ -536,16 +541,20 @@ static void launch_col2(bool adjoint, const WorkItem *items, int nitems, float2 
   }
 }
 
-void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
-                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
-{
-  launch_col2(true, items, nitems, grid, xs, perm, const_cast<float2 *>(f), g, poly, s);
-}
-
 void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
                    float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
-  launch_col2(false, items, nitems, const_cast<float2 *>(grid), xs, perm, f, g, poly, s);
+  if (nitems <= 0) return;
+  switch (g.w) {
+#define GB_C2_RUN(W)                                                \
+  case W:                                                           \
+    run_b2<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
+    return;
+    GB_COL2_WIDTHS(GB_C2_RUN)
+#undef GB_C2_RUN
+    default:
+      fatal("no 2-D column kernel for w=%d", g.w);
+  }
 }
 
 }  // namespace gb

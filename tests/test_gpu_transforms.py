@@ -252,23 +252,26 @@ def test_dense_3d_single(gpulib, density, m):
     assert rel_l2(gfh, rfh) < 2e-5, rel_l2(gfh, rfh)
 
 
-@pytest.mark.parametrize("m", [2, 3, 4, 5, 6, 7])
-def test_radial_2d_single(gpulib, m):
-    """2-D single precision on radial k-space lines: every spoke passes the
-    centre (one node repeated per spoke there), so the central tiles hold
-    hundreds of nodes per cell and split into many work items; every window
-    width of the 2-D column spreading kernel."""
+@pytest.mark.parametrize("m,single", [(2, True), (3, True), (4, True), (5, True), (6, True), (7, True),
+                                      (4, False), (6, False)])
+def test_radial_2d(gpulib, m, single):
+    """2-D radial k-space lines: every spoke passes the centre (one node
+    repeated per spoke there), so the central tiles hold hundreds of nodes
+    per cell and split into many work items; every window width of the
+    single-precision 2-D column kernels, and the double-precision column
+    spreading."""
     N = [64, 64]
     spokes, samples = 96, 128
     ang = np.pi * np.arange(spokes) / spokes
     r = -0.5 + np.arange(samples) / samples
     x = np.stack([np.outer(np.cos(ang), r).ravel(), np.outer(np.sin(ang), r).ravel()], axis=1)
-    x = (((x + 0.5) % 1.0) - 0.5).astype(np.float32)
+    x = (((x + 0.5) % 1.0) - 0.5).astype(np.float32 if single else np.float64)
     M = len(x)
     rng = np.random.default_rng(40 + m)
-    fh = (rng.uniform(-1, 1, 64 * 64) + 1j * rng.uniform(-1, 1, 64 * 64)).astype(np.complex64)
-    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
-    p = make_plan(gpulib, True, N, M, m=m)
+    ct = np.complex64 if single else np.complex128
+    fh = (rng.uniform(-1, 1, 64 * 64) + 1j * rng.uniform(-1, 1, 64 * 64)).astype(ct)
+    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(ct)
+    p = make_plan(gpulib, single, N, M, m=m)
     gf, gfh = run_both(p, x, fh, f)
     p.finalize()
     od = oracle.OraclePlan(N, M, n=[128, 128], m=m, single=False)
@@ -276,8 +279,9 @@ def test_radial_2d_single(gpulib, m):
     od.precompute()
     rf = od.trafo(fh)
     rfh = od.adjoint(f)
-    assert rel_l2(gf, rf) < 2e-5, rel_l2(gf, rf)
-    assert rel_l2(gfh, rfh) < 2e-5, rel_l2(gfh, rfh)
+    tol = 2e-5 if single else 1e-12
+    assert rel_l2(gf, rf) < tol, rel_l2(gf, rf)
+    assert rel_l2(gfh, rfh) < tol, rel_l2(gfh, rfh)
 
 
 def test_edge_nodes_and_small_m(gpulib):

@@ -144,6 +144,10 @@ int nfft_gb_mlp_adam(float *params, const float *grad, float *m1, float *m2, int
  * degree-9 interpolant, in double precision at the ten Chebyshev points of
  * [-1, 1], of phi(n x - (u + l)) with u = floor(n x) - m.  Host only. */
 void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef);
+/* The double-precision form of the 2-D double-precision kernels: coef[l * 17
+ * + k] (k < 17), the degree-16 interpolant at the 17 Chebyshev points,
+ * computed in extended precision and rounded to double.  Host only. */
+void nfft_gb_kb_polyd_fit(int m, double b, int w, double *coef);
 
 /* The node sort of NFFT_SORT_NODES without any device allocation (no
  * counterpart in the reference).  For callers that cannot allocate device

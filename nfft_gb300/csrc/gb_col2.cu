@@ -348,8 +348,8 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_b2_col(const WorkItem *__rest
 // The B^T above in double precision (the FP64 transforms of the
 // mixed-precision solver and of double plans): the same columns and lane
 // roles, FP64 accumulators (one FMA per y position and component), the
-// window evaluated exactly per node, four warps per CTA for the larger
-// vectors.
+// window from its degree-16 form (gb_window.cpp), four warps per CTA for the
+// larger vectors.
 static constexpr int C2D_THREADS = 128;
 static constexpr int C2D_WARPS = C2D_THREADS / 32;
 
@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(C2D_THREADS) k_bt2_col_d(const WorkItem *__res
                                                            double2 *__restrict__ grid,
                                                            const double *__restrict__ xs,
                                                            const uint32_t *__restrict__ perm,
-                                                           const double2 *__restrict__ f, Geom<double> g)
+                                                           const double2 *__restrict__ f, Geom<double> g,
+                                                           WinPolyD poly)
 {
   typedef C2<W> P;
   typedef C2D<W> Q;
@@ -397,8 +398,10 @@ __global__ void __launch_bounds__(C2D_THREADS) k_bt2_col_d(const WorkItem *__res
     int col = -1;
     if (lane < np) {
       const int i = a + lane;
-      const double x0 = xs[2LL * i], x1 = xs[2LL * i + 1];
-      const int u0 = node_u<double>(x0, g.nR[0], g.m), u1 = node_u<double>(x1, g.nR[1], g.m);
+      const double xn0 = xs[2LL * i] * g.nR[0], xn1 = xs[2LL * i + 1] * g.nR[1];
+      const int u0 = (int)floor(xn0) - g.m, u1 = (int)floor(xn1) - g.m;  // node_u
+      const double s0 = fma(2.0, xn0 - (double)u0, -(double)(2 * g.m + 1));
+      const double s1 = fma(2.0, xn1 - (double)u1, -(double)(2 * g.m + 1));
       const int ux = min(max(wrap(u0, g.n[0]) - org0, 0), C2_TILE - 1);
       const int uy = min(max(wrap(u1, g.n[1]) - org1, 0), C2_TILE - 1);
       const int ox = ux % CX, oy = uy % C2_CY;
@@ -408,13 +411,13 @@ __global__ void __launch_bounds__(C2D_THREADS) k_bt2_col_d(const WorkItem *__res
       double2 *xv = wx + Q::XS * lane;
 #pragma unroll
       for (int q = 0; q < 16; ++q) xv[q] = make_double2(0.0, 0.0);
-      node_psi<double, W>(x0, u0, g.nR[0], g.mm, g.b[0], v);
+      kb_polyd_taps_s<W>(s0, poly.c[0], v);
 #pragma unroll
       for (int l = 0; l < W; ++l) xv[ox + l] = make_double2(v[l] * fj.x, v[l] * fj.y);
       double *yv = wy + Q::YS * lane;
 #pragma unroll
       for (int q = 0; q < 2 * NP; ++q) yv[q] = 0.0;
-      node_psi<double, W>(x1, u1, g.nR[1], g.mm, g.b[1], v);
+      kb_polyd_taps_s<W>(s1, poly.c[1], v);
 #pragma unroll
       for (int l = 0; l < W; ++l) yv[oy + l] = v[l];
     }
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(C2D_THREADS) k_bt2_col_d(const WorkItem *__res
 
 template <int W>
 static void run_bt2_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
-                      const double2 *f, const Geom<double> &g, cudaStream_t s)
+                      const double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
 {
   static bool attr = false;
   const size_t smem = c2d_smem_bytes<W>();
@@ -478,8 +481,74 @@ static void run_bt2_d(const WorkItem *items, int nitems, double2 *grid, const do
     GB_CUDA(cudaFuncSetAttribute(k_bt2_col_d<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  k_bt2_col_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
+  k_bt2_col_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
   GB_LAUNCHED("bt2_col_d");
+}
+
+// Double-precision 2-D B, one node per thread over a 128-node work item: the
+// tile's padded subgrid in shared memory, the node's taps from the degree-16
+// form, the w^2 gather in row order.
+template <int W>
+__global__ void __launch_bounds__(C2D_THREADS) k_b2_node_d(const WorkItem *__restrict__ items,
+                                                           const double2 *__restrict__ grid,
+                                                           const double *__restrict__ xs,
+                                                           const uint32_t *__restrict__ perm,
+                                                           double2 *__restrict__ f, Geom<double> g, WinPolyD poly)
+{
+  typedef C2<W> P;
+  constexpr int EXT = P::EXT, SY = P::SY;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *const sg = reinterpret_cast<double2 *>(smem_raw);
+  const WorkItem it = items[blockIdx.x];
+  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  for (int idx = threadIdx.x; idx < EXT * EXT; idx += C2D_THREADS) {
+    const int rx = idx / EXT, ry = idx - rx * EXT;
+    int p0 = org0 + rx, p1 = org1 + ry;
+    while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+    while (p1 >= g.n[1]) p1 -= g.n[1];
+    sg[rx * SY + ry] = grid[(long long)p0 * g.n[1] + p1];
+  }
+  __syncthreads();
+  for (int i = it.start + threadIdx.x; i < it.end; i += C2D_THREADS) {
+    const double xn0 = xs[2LL * i] * g.nR[0], xn1 = xs[2LL * i + 1] * g.nR[1];
+    const int u0 = (int)floor(xn0) - g.m, u1 = (int)floor(xn1) - g.m;  // node_u
+    const double s0 = fma(2.0, xn0 - (double)u0, -(double)(2 * g.m + 1));
+    const double s1 = fma(2.0, xn1 - (double)u1, -(double)(2 * g.m + 1));
+    const int l0 = min(max(wrap(u0, g.n[0]) - org0, 0), C2_TILE - 1);
+    const int l1 = min(max(wrap(u1, g.n[1]) - org1, 0), C2_TILE - 1);
+    double v0[W], v1[W];
+    kb_polyd_taps_s<W>(s0, poly.c[0], v0);
+    kb_polyd_taps_s<W>(s1, poly.c[1], v1);
+    double ar = 0.0, ai = 0.0;
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      const double2 *row = sg + (l0 + a) * SY + l1;
+      double rr = 0.0, ri = 0.0;
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        const double2 c = row[b];
+        rr = fma(v1[b], c.x, rr);
+        ri = fma(v1[b], c.y, ri);
+      }
+      ar = fma(v0[a], rr, ar);
+      ai = fma(v0[a], ri, ai);
+    }
+    f[perm[i]] = make_double2(ar, ai);
+  }
+}
+
+template <int W>
+static void run_b2_d(const WorkItem *items, int nitems, const double2 *grid, const double *xs,
+                     const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
+{
+  static bool attr = false;
+  const size_t smem = (size_t)C2<W>::EXT * C2<W>::SY * sizeof(double2);
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(k_b2_node_d<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  k_b2_node_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
+  GB_LAUNCHED("b2_node_d");
 }
 
 template <int W>
@@ -562,18 +631,34 @@ void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const 
 namespace gb {
 
 void launch_bt2_col_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
-                      const double2 *f, const Geom<double> &g, cudaStream_t s)
+                      const double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
 {
   if (nitems <= 0) return;
   switch (g.w) {
-#define GB_C2D_RUN(W)                                         \
-  case W:                                                     \
-    run_bt2_d<W>(items, nitems, grid, xs, perm, f, g, s); \
+#define GB_C2D_RUN(W)                                               \
+  case W:                                                           \
+    run_bt2_d<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
     return;
     GB_COL2_WIDTHS(GB_C2D_RUN)
 #undef GB_C2D_RUN
     default:
       fatal("no 2-D column kernel for w=%d", g.w);
+  }
+}
+
+void launch_b2_node_d(const WorkItem *items, int nitems, const double2 *grid, const double *xs,
+                      const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
+{
+  if (nitems <= 0) return;
+  switch (g.w) {
+#define GB_C2D_RUN(W)                                              \
+  case W:                                                          \
+    run_b2_d<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
+    return;
+    GB_COL2_WIDTHS(GB_C2D_RUN)
+#undef GB_C2D_RUN
+    default:
+      fatal("no 2-D double-precision kernel for w=%d", g.w);
   }
 }
 

@@ -68,6 +68,13 @@ struct WinPoly {
 // fills coef[l * KB_POLY_DP + k] for the w taps of the window with cut-off m
 // and shape b (host, double precision)
 void kb_poly_fit(int m, double b, int w, float *coef);
+// The same in double precision for the 2-D double-precision kernels: degree
+// 16, interpolated in extended precision, within 5e-15 of the window's peak.
+#define KB_POLYD_DP 17
+struct WinPolyD {
+  double c[2][KB_POLY_WMAX][KB_POLYD_DP];  // per dimension, tap, increasing power of s
+};
+void kb_polyd_fit(int m, double b, int w, double *coef);
 
 struct WorkItem {
   int tile;    // linear tile id (row-major over ntile)
@@ -160,6 +167,21 @@ __device__ __forceinline__ void kb_poly_taps_s(float s, const float (&c)[KB_POLY
     float a = c[l][KB_POLY_DP - 1];
 #pragma unroll
     for (int k = KB_POLY_DP - 2; k >= 0; --k) a = fmaf(a, s, c[l][k]);
+    v[l] = a;
+  }
+}
+
+// double precision: the W taps of a node from the degree-16 form
+template <int W>
+__device__ __forceinline__ void kb_polyd_taps_s(double s, const double (&c)[KB_POLY_WMAX][KB_POLYD_DP],
+                                                double (&v)[W])
+{
+  static_assert(W <= KB_POLY_WMAX, "no polynomial form for this width");
+#pragma unroll
+  for (int l = 0; l < W; ++l) {
+    double a = c[l][KB_POLYD_DP - 1];
+#pragma unroll
+    for (int k = KB_POLYD_DP - 2; k >= 0; --k) a = fma(a, s, c[l][k]);
     v[l] = a;
   }
 }

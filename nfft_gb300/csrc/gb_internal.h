@@ -101,9 +101,12 @@ void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float
                     const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
 void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
                    float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
-// the B^T of the same layout in double precision
+// the B^T of the same layout in double precision, and a per-node B on the
+// same work items (both with the window's degree-16 form)
 void launch_bt2_col_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
-                      const double2 *f, const Geom<double> &g, cudaStream_t s);
+                      const double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s);
+void launch_b2_node_d(const WorkItem *items, int nitems, const double2 *grid, const double *xs,
+                      const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s);
 // generic global-memory kernels for any d and m
 template <typename R>
 void launch_b_generic(const typename Cx<R>::T *grid, const R *xs, const uint32_t *perm,

@@ -71,7 +71,8 @@ struct Ctx {
   bool tiled = false;
   bool group3 = false;  // 3-D sub-cell group kernels
   WinPoly poly = {};     // polynomial window of the single-precision 2-D / 3-D kernels
-  bool col2 = false;     // 2-D column B^T (and B in single precision); nodes keyed by column
+  WinPolyD polyd = {};   // the same in double precision (2-D double-precision kernels)
+  bool col2 = false;     // 2-D column kernels (nodes keyed by column)
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
@@ -406,6 +407,8 @@ static void init_help(typename Api<R>::plan *ths)
       kb_poly_fit(g.m, (double)ths->b[t], g.w, &c->poly.c[t][0][0]);
       if (ths->b[t] != ths->b[0]) c->poly.same = 0;
     }
+    if (std::is_same<R, double>::value && d == 2)
+      for (int t = 0; t < 2; ++t) kb_polyd_fit(g.m, (double)ths->b[t], g.w, &c->polyd.c[t][0][0]);
   }
   c->flags = ths->flags;
   choose_tiles<R>(c);
@@ -575,18 +578,18 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   return b;
 }
 
-// the 2-D column B where the plan selected it (single precision; double
-// keeps the per-node gather, whose FP64 arithmetic is the smaller); false
+// the 2-D column B where the plan selected it (double precision: a per-node
+// gather on the same work items, whose FP64 arithmetic is the smaller); false
 // otherwise
 template <typename R>
 static bool b2_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
-  if constexpr (std::is_same<R, float>::value) {
-    if (!c->col2) return false;
+  if (!c->col2) return false;
+  if constexpr (std::is_same<R, float>::value)
     launch_b2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
-    return true;
-  }
-  return false;
+  else
+    launch_b2_node_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->polyd, c->stream);
+  return true;
 }
 
 template <typename R>
@@ -616,7 +619,7 @@ static bool bt2_stage(Ctx<R> *c, const typename Cx<R>::T *f)
   if constexpr (std::is_same<R, float>::value)
     launch_bt2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
   else
-    launch_bt2_col_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->stream);
+    launch_bt2_col_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->polyd, c->stream);
   return true;
 }
 

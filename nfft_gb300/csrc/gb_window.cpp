@@ -1,5 +1,5 @@
 // gb_window.cpp -- per-tap polynomial form of the Kaiser-Bessel window for the
-// single-precision 3-D kernels.
+// single-precision 2-D / 3-D kernels and the double-precision 2-D kernels.
 //
 // The window (reference include/infft.h:209-215, with b = pi (2 - 1/sigma)
 // from include/infft.h:216-222) is evaluated at t = n x - (u + l) for the W
@@ -75,6 +75,58 @@ void kb_poly_fit(int m, double b, int w, float *coef)
   }
 }
 
+// Double-precision form: the tap functions are sampled in extended precision
+// (long double) at the KB_POLYD_DP Chebyshev points of [-1, 1], their
+// Chebyshev coefficients taken by the discrete cosine sums, converted to
+// monomial coefficients by the three-term recurrence T_{k+1} = 2 s T_k -
+// T_{k-1}, all in long double, and rounded to double once.
+static long double kb_phi_ext(long double t, int m, long double b)
+{
+  const long double a = (long double)m * m - t * t;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  if (a > 0) {
+    const long double s = sqrtl(a);
+    return sinhl(b * s) / (pi * s);
+  }
+  if (a < 0) {
+    const long double s = sqrtl(-a);
+    return sinl(b * s) / (pi * s);
+  }
+  return b / pi;
+}
+
+void kb_polyd_fit(int m, double b, int w, double *coef)
+{
+  const int n = KB_POLYD_DP;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  long double xk[KB_POLYD_DP], yk[KB_POLYD_DP], ch[KB_POLYD_DP];
+  long double tprev[KB_POLYD_DP], tcur[KB_POLYD_DP], tnext[KB_POLYD_DP], mono[KB_POLYD_DP];
+  for (int k = 0; k < n; ++k) xk[k] = cosl(pi * (k + 0.5L) / n);
+  for (int l = 0; l < w; ++l) {
+    for (int k = 0; k < n; ++k) yk[k] = kb_phi_ext(0.5L * (xk[k] + 1.0L) + m - l, m, (long double)b);
+    for (int j = 0; j < n; ++j) {
+      long double s = 0;
+      for (int k = 0; k < n; ++k) s += yk[k] * cosl(pi * j * (k + 0.5L) / n);
+      ch[j] = s * (j == 0 ? 1.0L : 2.0L) / n;
+    }
+    for (int k = 0; k < n; ++k) tprev[k] = tcur[k] = mono[k] = 0;
+    tprev[0] = 1;  // T_0
+    tcur[1] = 1;   // T_1
+    mono[0] = ch[0];
+    for (int k = 0; k < n; ++k) mono[k] += ch[1] * tcur[k];
+    for (int j = 2; j < n; ++j) {
+      for (int k = 0; k < n; ++k) tnext[k] = (k > 0 ? 2 * tcur[k - 1] : 0) - tprev[k];
+      for (int k = 0; k < n; ++k) {
+        mono[k] += ch[j] * tnext[k];
+        tprev[k] = tcur[k];
+        tcur[k] = tnext[k];
+      }
+    }
+    for (int k = 0; k < n; ++k) coef[l * n + k] = (double)mono[k];
+  }
+}
+
 }  // namespace gb
 
 extern "C" void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef) { gb::kb_poly_fit(m, b, w, coef); }
+extern "C" void nfft_gb_kb_polyd_fit(int m, double b, int w, double *coef) { gb::kb_polyd_fit(m, b, w, coef); }

@@ -55,3 +55,30 @@ def test_polynomial_window_matches_kaiser_bessel(m, sigma):
         worst = max(worst, np.max(np.abs(horner_f32(c[l], s) - exact)) / peak)
     # single-precision rounding of the window's peak is 6e-8 of it
     assert worst < 2e-7, worst
+
+
+@pytest.mark.parametrize("m,sigma", [(2, 2.0), (4, 2.0), (5, 1.5), (6, 2.0), (7, 2.0), (6, 1.25)])
+def test_double_polynomial_window_matches_kaiser_bessel(m, sigma):
+    """The degree-16 form of the double-precision 2-D kernels: Horner in
+    double precision within 1e-14 of the window's peak (the kernels' taps
+    then agree with the exact window to the last few digits)."""
+    lib = nfft_gb300.lib()
+    fit = lib.nfft_gb_kb_polyd_fit
+    fit.restype = None
+    fit.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_double)]
+    w = 2 * m + 2
+    b = np.pi * (2.0 - 1.0 / sigma)
+    coef = (C.c_double * (w * 17))()
+    fit(m, b, w, coef)
+    c = np.ctypeslib.as_array(coef).reshape(w, 17)
+    rng = np.random.default_rng(m)
+    frac = np.concatenate([rng.uniform(0, 1, 4000), [0.0, 0.5, 1.0 - 2.0 ** -52]])
+    s = 2.0 * frac - 1.0
+    peak = kb_phi(np.array([0.0]), m, b)[0]
+    worst = 0.0
+    for l in range(w):
+        v = np.zeros_like(s)
+        for a in c[l][::-1]:
+            v = v * s + a
+        worst = max(worst, np.max(np.abs(v - kb_phi(frac + m - l, m, b))) / peak)
+    assert worst < 1e-14, worst

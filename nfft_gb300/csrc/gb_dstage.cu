@@ -8,8 +8,9 @@
 //
 // Frequency k_t in [-N_t/2, N_t/2) sits at FFT-order grid position
 // k_t mod n_t; every other grid point of the trafo input is zero.  The pad
-// kernel writes the whole n_total grid in one coalesced pass, so no separate
-// memset of the grid is needed.
+// zeroes the grid with a memset and scatters the N_total scaled
+// coefficients, one thread per frequency (reads and writes coalesced along
+// the last dimension); the crop gathers them back.
 #include "gb_internal.h"
 
 namespace gb {
@@ -39,12 +40,8 @@ void launch_cphi(const Geom<R> &g, double *cphi, cudaStream_t s)
   GB_LAUNCHED("cphi");
 }
 
-// Row-wise D and D^T.  A block owns (part of) one grid row along the last
-// dimension: the row's position in the other dimensions, whether it meets
-// the frequency box and the product of their FP64 coefficients are computed
-// once per block with 32-bit index arithmetic; threads then stride along the
-// row with coalesced loads and stores.  In single precision the FP64
-// coefficient product is rounded once to float and applied in float.
+// In single precision the FP64 coefficient product is rounded once to float
+// and applied in float.
 template <typename R>
 __device__ __forceinline__ typename Cx<R>::T d_scale(typename Cx<R>::T v, double c);
 template <>
@@ -59,131 +56,86 @@ __device__ __forceinline__ double2 d_scale<double>(double2 v, double c)
   return make_double2(v.x * c, v.y * c);
 }
 
-// Natural-order index kk of grid position i (FFT order) along a dimension of
-// length n with bandwidth N, or -1 outside the frequency box.
-__device__ __forceinline__ int d_natural(int i, int n, int N)
-{
-  const int k = (i < n / 2) ? i : i - n;
-  const int kk = k + N / 2;
-  return (kk >= 0 && kk < N) ? kk : -1;
-}
-
-// Grid row r (over dims 0..d-2 of n) -> whether it meets the frequency box,
-// the natural-order row of f_hat it holds and the FP64 coefficient product.
+// FFT-order grid index of natural frequency index k (row-major over N) and
+// the FP64 coefficient product, formed in the order the row-wise form used:
+// dims d-2 .. 0 from 1.0, then the last dimension.
 template <typename R>
-__device__ __forceinline__ bool d_pad_row(unsigned r, const Geom<R> &g, const double *cphi, long long &frow,
-                                          double &c)
+__device__ __forceinline__ long long d_point(long long k, const Geom<R> &g, const double *__restrict__ cphi,
+                                             double &c)
 {
-  bool inside = true;
-  long long fmul = 1;
+  int kk[GB_MAXD];
+  if (g.N_total <= 0xffffffffLL) {  // 32-bit division where the index fits
+    unsigned r = (unsigned)k;
+    for (int t = g.d - 1; t >= 0; --t) {
+      const unsigned q = r / (unsigned)g.N[t];
+      kk[t] = (int)(r - q * (unsigned)g.N[t]);
+      r = q;
+    }
+  } else {
+    for (int t = g.d - 1; t >= 0; --t) {
+      const long long q = k / g.N[t];
+      kk[t] = (int)(k - q * g.N[t]);
+      k = q;
+    }
+  }
   int off = 0;
   for (int t = 0; t < g.d - 1; ++t) off += g.N[t];
-  frow = 0;
+  const int offl = off;
   c = 1.0;
   for (int t = g.d - 2; t >= 0; --t) {
-    const unsigned nt = (unsigned)g.n[t];
-    const unsigned q = r / nt;
-    const int i = (int)(r - q * nt);
-    r = q;
     off -= g.N[t];
-    const int kk = d_natural(i, g.n[t], g.N[t]);
-    if (kk < 0) inside = false;
-    else c *= cphi[off + kk];
-    frow += fmul * kk;
-    fmul *= g.N[t];
+    c *= cphi[off + kk[t]];
   }
-  return inside;
+  c = c * cphi[offl + kk[g.d - 1]];
+  long long gi = 0;
+  for (int t = 0; t < g.d; ++t) {
+    const int f = kk[t] - g.N[t] / 2;
+    gi = gi * g.n[t] + (f < 0 ? f + g.n[t] : f);
+  }
+  return gi;
 }
 
-// Row r of f_hat (over dims 0..d-2 of N) -> the grid row holding it and the
-// FP64 coefficient product.
-template <typename R>
-__device__ __forceinline__ long long d_crop_row(unsigned r, const Geom<R> &g, const double *cphi, double &c)
-{
-  long long grow = 0, gmul = 1;
-  int off = 0;
-  for (int t = 0; t < g.d - 1; ++t) off += g.N[t];
-  c = 1.0;
-  for (int t = g.d - 2; t >= 0; --t) {
-    const unsigned Nt = (unsigned)g.N[t];
-    const unsigned q = r / Nt;
-    const int kk = (int)(r - q * Nt);
-    r = q;
-    off -= g.N[t];
-    const int k = kk - g.N[t] / 2;
-    c *= cphi[off + kk];
-    grow += gmul * (k < 0 ? k + g.n[t] : k);
-    gmul *= g.n[t];
-  }
-  return grow;
-}
-
-// Trafo: g = f_hat(k) prod_t c_t inside the frequency box, zero elsewhere;
-// writes the whole n_total grid (no separate memset).  Blocks stride over
-// the grid rows.
+// Trafo: g = f_hat(k) prod_t c_t inside the frequency box (the grid is
+// zeroed before by a memset); one thread per frequency.
 template <typename R>
 __global__ void __launch_bounds__(256) k_d_pad(const typename Cx<R>::T *__restrict__ fhat,
                                                const double *__restrict__ cphi,
                                                typename Cx<R>::T *__restrict__ grid, Geom<R> g)
 {
-  typedef typename Cx<R>::T C;
-  const int nl = g.n[g.d - 1], Nl = g.N[g.d - 1];
-  const double *cl = cphi;
-  for (int t = 0; t < g.d - 1; ++t) cl += g.N[t];
-  const unsigned rows = (unsigned)(g.n_total / nl);
-  for (unsigned r = blockIdx.x; r < rows; r += gridDim.x) {
-    long long frow;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < g.N_total;
+       k += (long long)gridDim.x * blockDim.x) {
     double c;
-    const bool inside = d_pad_row<R>(r, g, cphi, frow, c);
-    C *row = grid + (long long)r * nl;
-    const C *src = fhat + frow * Nl;
-    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < nl; i += gridDim.y * blockDim.x) {
-      C out = cmake(R(0), R(0));
-      const int kk = d_natural(i, nl, Nl);
-      if (inside && kk >= 0) out = d_scale<R>(src[kk], c * cl[kk]);
-      row[i] = out;
-    }
+    const long long gi = d_point<R>(k, g, cphi, c);
+    grid[gi] = d_scale<R>(fhat[k], c);
   }
 }
 
-// Adjoint: f_hat(k) = g(k mod n) prod_t c_t.  Blocks stride over the rows
-// of f_hat.
+// Adjoint: f_hat(k) = g(k mod n) prod_t c_t; one thread per frequency.
 template <typename R>
 __global__ void __launch_bounds__(256) k_d_crop(const typename Cx<R>::T *__restrict__ grid,
                                                 const double *__restrict__ cphi,
                                                 typename Cx<R>::T *__restrict__ fhat, Geom<R> g)
 {
-  typedef typename Cx<R>::T C;
-  const int nl = g.n[g.d - 1], Nl = g.N[g.d - 1];
-  const double *cl = cphi;
-  for (int t = 0; t < g.d - 1; ++t) cl += g.N[t];
-  const unsigned rows = (unsigned)(g.N_total / Nl);
-  for (unsigned r = blockIdx.x; r < rows; r += gridDim.x) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < g.N_total;
+       k += (long long)gridDim.x * blockDim.x) {
     double c;
-    const C *src = grid + d_crop_row<R>(r, g, cphi, c) * nl;
-    C *out = fhat + (long long)r * Nl;
-    for (int kk = blockIdx.y * blockDim.x + threadIdx.x; kk < Nl; kk += gridDim.y * blockDim.x) {
-      const int k = kk - Nl / 2;
-      out[kk] = d_scale<R>(src[k < 0 ? k + nl : k], c * cl[kk]);
-    }
+    const long long gi = d_point<R>(k, g, cphi, c);
+    fhat[k] = d_scale<R>(grid[gi], c);
   }
 }
 
-// blocks stride over rows (at most 16 resident blocks' worth per SM)
-static dim3 d_rows_grid(long long rows, int len, int th)
+static unsigned d_blocks(long long n)
 {
-  const long long chunks = (len + th - 1) / th;
-  const long long bx = rows < 152 * 16 ? rows : 152 * 16;
-  return dim3((unsigned)bx, (unsigned)(chunks < 65535 ? chunks : 65535), 1);
+  const long long b = (n + 255) / 256;
+  return (unsigned)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
 }
 
 template <typename R>
 void launch_d_pad(const typename Cx<R>::T *fhat, const double *cphi, typename Cx<R>::T *grid,
                   const Geom<R> &g, cudaStream_t s)
 {
-  const int th = 256;
-  const int nl = g.n[g.d - 1];
-  k_d_pad<R><<<d_rows_grid(g.n_total / nl, nl, th), th, 0, s>>>(fhat, cphi, grid, g);
+  GB_CUDA(cudaMemsetAsync(grid, 0, (size_t)g.n_total * sizeof(typename Cx<R>::T), s));
+  k_d_pad<R><<<d_blocks(g.N_total), 256, 0, s>>>(fhat, cphi, grid, g);
   GB_LAUNCHED("d_pad");
 }
 
@@ -191,9 +143,7 @@ template <typename R>
 void launch_d_crop(const typename Cx<R>::T *grid, const double *cphi, typename Cx<R>::T *fhat,
                    const Geom<R> &g, cudaStream_t s)
 {
-  const int th = 256;
-  const int Nl = g.N[g.d - 1];
-  k_d_crop<R><<<d_rows_grid(g.N_total / Nl, Nl, th), th, 0, s>>>(grid, cphi, fhat, g);
+  k_d_crop<R><<<d_blocks(g.N_total), 256, 0, s>>>(grid, cphi, fhat, g);
   GB_LAUNCHED("d_crop");
 }
 

@@ -23,8 +23,7 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
         GB_CUDA(cudaFuncSetAttribute(k_bt3_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr_col = true;
       }
-      launch_gather_c(f, perm, g.M, cb.fs, s);
-      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, cb.fs, g, poly);
+      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly);
       GB_LAUNCHED("bt3_col");
       return;
     }

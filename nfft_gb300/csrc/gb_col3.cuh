@@ -21,7 +21,8 @@
 // tile's padded subgrid in shared memory as interleaved complex values.  A
 // warp takes a column chunk (at most 32 nodes of one column):
 //  * lane j evaluates node j's window into per-warp vectors: x scaled by f_j
-//    (complex), y, and z duplicated as (w, w) pairs;
+//    (complex; f_j read through the node permutation, the one scattered read
+//    of the adjoint), y, and z duplicated as (w, w) pairs;
 //  * lanes own (x, y) rows of the column (two per lane) and hold all
 //    8 + W - 1 z values of a row as complex accumulators in registers; for the
 //    nodes whose window starts at z0 (a compile-time case, eight of them)
@@ -147,7 +148,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
                                                             float2 *__restrict__ grid,
                                                             const float4 *__restrict__ rec,
                                                             const uint16_t *__restrict__ cst,
-                                                            const float2 *__restrict__ fs, Geom<float> g,
+                                                            const uint32_t *__restrict__ perm,
+                                                            const float2 *__restrict__ f, Geom<float> g,
                                                             WinPoly poly)
 {
   typedef C3<W> P;
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   }
   if (threadIdx.x == 0) {
     c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
-    c3_prefetch_l2(fs + it.start, 8LL * (it.end - it.start));
+    c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
   }
   for (int i = threadIdx.x; i < EXT * g.sx2; i += C3_THREADS) sg[i] = make_float2(0.f, 0.f);
   // column boundaries of the item (node set-up): cstart[c] = first node of column c
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     int z0 = 8;
     if (lane < np) {
       const float4 r = rec[a + lane];
-      const float2 fj = fs[a + lane];
+      const float2 fj = f[perm[a + lane]];
       const int loc = __float_as_int(r.w);
       float v[W];
       // x, scaled by f_j, at the node's offset in the column's box

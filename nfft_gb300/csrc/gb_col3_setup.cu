@@ -1,6 +1,5 @@
 // gb_col3_setup.cu -- node set-up for the single-precision 3-D kernels of
-// gb_col3.cuh, done once per node set (in precompute_one_psi), and the
-// per-call gather of the adjoint's input into tile order.
+// gb_col3.cuh, done once per node set (in precompute_one_psi).
 //
 // The reference precomputes per-node window data once per node set as well
 // (PRE_PSI tables, nfft.c:5819-5844); here a node keeps 16 bytes: its three
@@ -47,12 +46,6 @@ __global__ void k_c3_item_starts(const WorkItem *__restrict__ items, const uint3
   }
 }
 
-__global__ void k_gather_c(const float2 *__restrict__ f, const uint32_t *__restrict__ perm, long long M,
-                           float2 *__restrict__ fs)
-{
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < M) fs[i] = f[perm[i]];
-}
 
 void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *items, int nitems,
                      const uint32_t *keys, float4 *rec, uint16_t *cst, uint16_t *sst, cudaStream_t s)
@@ -67,11 +60,5 @@ void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *item
   }
 }
 
-void launch_gather_c(const float2 *f, const uint32_t *perm, long long M, float2 *fs, cudaStream_t s)
-{
-  if (M <= 0) return;
-  k_gather_c<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(f, perm, M, fs);
-  GB_LAUNCHED("gather_c");
-}
 
 }  // namespace gb

@@ -79,11 +79,9 @@ struct Col3Bufs {
   const float4 *rec;    // per sorted node: s_0, s_1, s_2, packed window starts in the tile
   const uint16_t *cst;  // per work item: 17 column starts
   const uint16_t *sst;  // per work item: 65 sub-cell starts
-  float2 *fs;           // adjoint input in tile order (M values)
 };
 void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *items, int nitems,
                      const uint32_t *keys, float4 *rec, uint16_t *cst, uint16_t *sst, cudaStream_t s);
-void launch_gather_c(const float2 *f, const uint32_t *perm, long long M, float2 *fs, cudaStream_t s);
 int group3_max_item();
 template <typename R>
 void launch_b3_group(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,

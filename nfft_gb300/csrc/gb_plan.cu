@@ -76,7 +76,6 @@ struct Ctx {
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
-  C *fs = nullptr;       // adjoint input in tile order
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // FFT: one plan for d <= 3; for d > 3 a rank-3 plan over the last three
@@ -436,7 +435,6 @@ static void init_help(typename Api<R>::plan *ths)
       dev_alloc<R>((void **)&c->c3rec, M * sizeof(float4));
       dev_alloc<R>((void **)&c->c3cst, cap * 17 * sizeof(uint16_t));
       dev_alloc<R>((void **)&c->c3sst, cap * 65 * sizeof(uint16_t));
-      dev_alloc<R>((void **)&c->fs, M * sizeof(C));
     }
     make_fft<R>(c);
   }
@@ -574,7 +572,6 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   b.rec = c->c3rec;
   b.cst = c->c3cst;
   b.sst = c->c3sst;
-  b.fs = reinterpret_cast<float2 *>(c->fs);
   return b;
 }
 
@@ -876,7 +873,6 @@ static void finalize(typename Api<R>::plan *ths)
     cudaFree(c->c3rec);
     cudaFree(c->c3cst);
     cudaFree(c->c3sst);
-    cudaFree(c->fs);
     for (int i = 0; i < 7; ++i)
       if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (cudaEvent_t e : c->ring) cudaEventDestroy(e);

@@ -99,8 +99,9 @@ int nfft_gb_device_ok(void);
  * device f, adjoint reads the device f and writes the device f_hat.
  *  - create / destroy a batch over `count` plans (the plans must outlive it);
  *  - autotune: per class of plans (m, oversampling, node density) choose the
- *    tile edge (8, 16, 32) and threads per node (1, 4, 16) by timing; the
- *    choice is remembered for the process;
+ *    tile edge (8, 16, 32) and threads per node (1, 4, 16), or the 2-D column
+ *    kernels on 32^2 tiles (reported as T = 32, threads per node 0), by
+ *    timing; the choice is remembered for the process;
  *  - run: what = 1 trafo, 2 adjoint, 3 both; mode 0 = stream launches, 1 = a
  *    CUDA graph of trafo + adjoint captured on first use (what must be 3);
  *    returns after the GPU has finished;
@@ -113,6 +114,11 @@ float nfftf_gb_batch_time(void *batch, int reps, int mode);
 long long nfftf_gb_batch_nodes(void *batch);
 int nfftf_gb_batch_items(void *batch);
 int nfftf_gb_batch_plan_config(void *batch, int k, int *T, int *tpn);
+/* Set plan k's configuration by hand (T in {8, 16, 32} with threads per node
+ * in {1, 4, 16}, or T = 32 with 0 for the column kernels); re-bins the plan's
+ * nodes and rebuilds the batch tables.  Returns -1 for other values or a plan
+ * the column kernels cannot take. */
+int nfftf_gb_batch_set_config(void *batch, int k, int T, int tpn);
 
 /* Density-compensation weights for the inverse NFFT (no counterpart in the
  * reference, whose solver takes the weights w from the caller):

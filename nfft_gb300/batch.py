@@ -43,6 +43,7 @@ class Batch:
         self._items = _fn(lib, "nfftf_gb_batch_items", C.c_int, [vp])
         self._cfg = _fn(lib, "nfftf_gb_batch_plan_config", C.c_int,
                         [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)])
+        self._set_cfg = _fn(lib, "nfftf_gb_batch_set_config", C.c_int, [vp, C.c_int, C.c_int, C.c_int])
         arr = (vp * len(plans))(*[C.addressof(p.p) for p in plans])
         self.h = self._create(arr, len(plans))
         if not self.h:
@@ -69,6 +70,11 @@ class Batch:
         T, tpn = C.c_int(), C.c_int()
         self._cfg(self.h, k, C.byref(T), C.byref(tpn))
         return T.value, tpn.value
+
+    def set_config(self, k, T, tpn):
+        """Plan k on tiles of edge T with tpn threads per node, or (32, 0)
+        for the column kernels; returns the library's status (0 = done)."""
+        return self._set_cfg(self.h, k, T, tpn)
 
     def close(self):
         if self.h:

@@ -18,7 +18,12 @@ struct Batch {
   long long *d_grid_off = nullptr, *d_fhat_off = nullptr;
   BItem *d_items = nullptr;
   int nitems = 0;
-  int *d_counter = nullptr;  // [0] B queue head, [1] B^T queue head
+  BItem *d_items_col = nullptr;  // items of the plans in column mode
+  int nitems_col = 0;
+  WinPoly *d_polys = nullptr;    // the plans' polynomial windows
+  size_t smem_col = 0;
+  int grid_ctas_col = 0;
+  int *d_counter = nullptr;  // [0] B queue head, [1] B^T queue head, [2], [3] the same for column items
   float2 *arena = nullptr;
   long long arena_total = 0, fhat_total = 0;
   std::vector<FftGroup> ffts;
@@ -40,10 +45,13 @@ static void check_fft_b(cufftResult r, const char *what)
 static void batch_tables(Batch *b)
 {
   const int np = (int)b->plans.size();
-  std::vector<BItem> items;
+  std::vector<BItem> items, items_col;
   std::vector<long long> goff(np), foff(np);
+  std::vector<WinPoly> polys(np);
   b->total_nodes = 0;
-  size_t smem = 0;
+  size_t smem = 0, smem_col = 0;
+  if (b->d_polys) GB_CUDA(cudaFree(b->d_polys));
+  GB_CUDA(cudaMalloc(&b->d_polys, sizeof(WinPoly) * std::max(np, 1)));
   for (int k = 0; k < np; ++k) {
     PlanViewF v;
     plan_view_f(b->plans[k], &v);
@@ -51,8 +59,11 @@ static void batch_tables(Batch *b)
       fatal("batch: plan %d is not a 2-D tiled plan with nodes set up", k);
     if (v.g.w != 10 && v.g.w != 14) fatal("batch: plan %d has m=%d (batched kernels take m = 4 or 6)", k, v.g.m);
     BPlan &P = b->host_plans[k];
-    const int tpn = P.tpn ? P.tpn : 1;
+    // tpn 0 asks for the column kernels, which need the plan's nodes keyed by column
+    const int tpn = (P.tpn == 0 && !v.col2) ? 1 : P.tpn;
     memset(&P, 0, sizeof(P));
+    polys[k] = *v.poly;
+    P.poly = b->d_polys + k;
     P.g = v.g;
     P.xs = v.xs;
     P.perm = v.perm;
@@ -63,11 +74,15 @@ static void batch_tables(Batch *b)
     P.fhat_out = v.fhat;
     P.tpn = tpn;
     b->total_nodes += v.g.M;
-    smem = std::max(smem, (size_t)v.g.ext[0] * v.g.ext[1] * sizeof(float2));
+    if (tpn == 0)
+      smem_col = std::max({smem_col, v.g.w == 10 ? c2_smem_bytes<10>(true) : c2_smem_bytes<14>(true),
+                           v.g.w == 10 ? c2_smem_bytes<10>(false) : c2_smem_bytes<14>(false)});
+    else
+      smem = std::max(smem, (size_t)v.g.ext[0] * v.g.ext[1] * sizeof(float2));
     std::vector<WorkItem> wi(v.nitems);
     if (v.nitems)
       GB_CUDA(cudaMemcpy(wi.data(), v.items, sizeof(WorkItem) * v.nitems, cudaMemcpyDeviceToHost));
-    for (const WorkItem &w : wi) items.push_back(BItem{k, w.tile, w.start, w.end});
+    for (const WorkItem &w : wi) (tpn == 0 ? items_col : items).push_back(BItem{k, w.tile, w.start, w.end});
   }
   // grids of equal shape are contiguous in the arena, one batched FFT per shape
   std::map<std::pair<int, int>, std::vector<int>> shapes;
@@ -113,11 +128,18 @@ static void batch_tables(Batch *b)
     check_fft_b(cufftSetStream(fg.h, b->stream), "stream");
   }
   // largest items first: the persistent kernels then end with small work
-  std::stable_sort(items.begin(), items.end(),
-                   [](const BItem &a, const BItem &c) { return (a.end - a.start) > (c.end - c.start); });
+  auto larger = [](const BItem &a, const BItem &c) { return (a.end - a.start) > (c.end - c.start); };
+  std::stable_sort(items.begin(), items.end(), larger);
+  std::stable_sort(items_col.begin(), items_col.end(), larger);
   b->nitems = (int)items.size();
+  b->nitems_col = (int)items_col.size();
+  GB_CUDA(cudaMemcpy(b->d_polys, polys.data(), sizeof(WinPoly) * np, cudaMemcpyHostToDevice));
   if (b->d_plans) GB_CUDA(cudaFree(b->d_plans));
   if (b->d_items) GB_CUDA(cudaFree(b->d_items));
+  if (b->d_items_col) GB_CUDA(cudaFree(b->d_items_col));
+  GB_CUDA(cudaMalloc(&b->d_items_col, sizeof(BItem) * std::max(b->nitems_col, 1)));
+  if (b->nitems_col)
+    GB_CUDA(cudaMemcpy(b->d_items_col, items_col.data(), sizeof(BItem) * b->nitems_col, cudaMemcpyHostToDevice));
   if (b->d_grid_off) GB_CUDA(cudaFree(b->d_grid_off));
   if (b->d_fhat_off) GB_CUDA(cudaFree(b->d_fhat_off));
   // device table: [0, np) by plan index (B, B^T, crop), [np, 2np) in arena order (pad)
@@ -140,6 +162,16 @@ static void batch_tables(Batch *b)
   GB_CUDA(cudaGetDevice(&dev));
   GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   b->grid_ctas = std::max(1, per_sm) * sms;
+  b->smem_col = smem_col;
+  b->grid_ctas_col = 0;
+  if (b->nitems_col) {
+    GB_CUDA(cudaFuncSetAttribute(k_batch_b2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+    GB_CUDA(cudaFuncSetAttribute(k_batch_bt2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+    int per_sm_c = 0, per_sm_c2 = 0;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, k_batch_bt2c, C2_THREADS, smem_col));
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c2, k_batch_b2c, C2_THREADS, smem_col));
+    b->grid_ctas_col = std::max(1, std::min(per_sm_c, per_sm_c2)) * sms;
+  }
   if (b->graph_exec) {
     cudaGraphExecDestroy(b->graph_exec);
     b->graph_exec = nullptr;
@@ -162,9 +194,17 @@ static void batch_trafo_enqueue(Batch *b)
     check_fft_b(cufftExecC2C(fg.h, (cufftComplex *)(b->arena + fg.off), (cufftComplex *)(b->arena + fg.off),
                              CUFFT_FORWARD),
                 "exec");
-  GB_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
-  k_batch_b2<<<b->grid_ctas, BT_THREADS, b->smem, s>>>(b->d_plans, b->d_items, b->nitems, b->d_counter);
-  GB_LAUNCHED("batch_b2");
+  if (b->nitems) {
+    GB_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
+    k_batch_b2<<<b->grid_ctas, BT_THREADS, b->smem, s>>>(b->d_plans, b->d_items, b->nitems, b->d_counter);
+    GB_LAUNCHED("batch_b2");
+  }
+  if (b->nitems_col) {
+    GB_CUDA(cudaMemsetAsync(b->d_counter + 2, 0, sizeof(int), s));
+    k_batch_b2c<<<b->grid_ctas_col, C2_THREADS, b->smem_col, s>>>(b->d_plans, b->d_items_col, b->nitems_col,
+                                                                  b->d_counter + 2);
+    GB_LAUNCHED("batch_b2c");
+  }
 }
 
 // f_hat = A^H f for every plan
@@ -173,9 +213,17 @@ static void batch_adjoint_enqueue(Batch *b)
   const int np = (int)b->plans.size();
   cudaStream_t s = b->stream;
   GB_CUDA(cudaMemsetAsync(b->arena, 0, sizeof(float2) * b->arena_total, s));
-  GB_CUDA(cudaMemsetAsync(b->d_counter + 1, 0, sizeof(int), s));
-  k_batch_bt2<<<b->grid_ctas, BT_THREADS, b->smem, s>>>(b->d_plans, b->d_items, b->nitems, b->d_counter + 1);
-  GB_LAUNCHED("batch_bt2");
+  if (b->nitems) {
+    GB_CUDA(cudaMemsetAsync(b->d_counter + 1, 0, sizeof(int), s));
+    k_batch_bt2<<<b->grid_ctas, BT_THREADS, b->smem, s>>>(b->d_plans, b->d_items, b->nitems, b->d_counter + 1);
+    GB_LAUNCHED("batch_bt2");
+  }
+  if (b->nitems_col) {
+    GB_CUDA(cudaMemsetAsync(b->d_counter + 3, 0, sizeof(int), s));
+    k_batch_bt2c<<<b->grid_ctas_col, C2_THREADS, b->smem_col, s>>>(b->d_plans, b->d_items_col, b->nitems_col,
+                                                                   b->d_counter + 3);
+    GB_LAUNCHED("batch_bt2c");
+  }
   for (auto &fg : b->ffts)
     check_fft_b(cufftExecC2C(fg.h, (cufftComplex *)(b->arena + fg.off), (cufftComplex *)(b->arena + fg.off),
                              CUFFT_INVERSE),
@@ -198,8 +246,9 @@ static void batch_capture(Batch *b)
 
 // ------------------------------------------------------------ autotuner
 // Per class of plans (m, sigma, node density) the tile edge T in {8, 16, 32}
-// and the threads per node in {1, 4, 16} with the shortest B + B^T time,
-// measured on up to four plans of the class run as their own batch.
+// and the threads per node in {1, 4, 16}, or the column kernels on 32^2 tiles
+// (T = 0, tpn = 0), with the shortest B + B^T time, measured on up to four
+// plans of the class run as their own batch.
 struct TuneKey {
   int w, sigma100, dens;
   bool operator<(const TuneKey &o) const
@@ -229,12 +278,20 @@ static float time_b_pair(Batch *b, int reps)
   batch_adjoint_enqueue(b);
   GB_CUDA(cudaEventRecord(b->ev[0], b->stream));
   for (int r = 0; r < reps; ++r) {
-    GB_CUDA(cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(int), b->stream));
+    GB_CUDA(cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(int), b->stream));
     k_batch_b2<<<b->grid_ctas, BT_THREADS, b->smem, b->stream>>>(b->d_plans, b->d_items, b->nitems, b->d_counter);
     GB_LAUNCHED("batch_b2");
     k_batch_bt2<<<b->grid_ctas, BT_THREADS, b->smem, b->stream>>>(b->d_plans, b->d_items, b->nitems,
                                                                   b->d_counter + 1);
     GB_LAUNCHED("batch_bt2");
+    if (b->nitems_col) {
+      k_batch_b2c<<<b->grid_ctas_col, C2_THREADS, b->smem_col, b->stream>>>(b->d_plans, b->d_items_col,
+                                                                            b->nitems_col, b->d_counter + 2);
+      GB_LAUNCHED("batch_b2c");
+      k_batch_bt2c<<<b->grid_ctas_col, C2_THREADS, b->smem_col, b->stream>>>(b->d_plans, b->d_items_col,
+                                                                             b->nitems_col, b->d_counter + 3);
+      GB_LAUNCHED("batch_bt2c");
+    }
   }
   GB_CUDA(cudaEventRecord(b->ev[1], b->stream));
   GB_CUDA(cudaEventSynchronize(b->ev[1]));
@@ -250,7 +307,7 @@ static Batch *batch_new(nfftf_plan **plans, int count)
   b->host_plans.resize(count);
   for (auto &P : b->host_plans) P.tpn = 1;
   GB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-  GB_CUDA(cudaMalloc(&b->d_counter, 2 * sizeof(int)));
+  GB_CUDA(cudaMalloc(&b->d_counter, 4 * sizeof(int)));
   for (int i = 0; i < 8; ++i) GB_CUDA(cudaEventCreate(&b->ev[i]));
   for (auto *p : b->plans) GB_CUDA(cudaStreamSynchronize((cudaStream_t)nfftf_gb_get_stream(p)));
   batch_tables(b);
@@ -266,6 +323,8 @@ static void batch_free(Batch *b)
   for (auto &fg : b->ffts) cufftDestroy(fg.h);
   cudaFree(b->d_plans);
   cudaFree(b->d_items);
+  cudaFree(b->d_items_col);
+  cudaFree(b->d_polys);
   cudaFree(b->d_grid_off);
   cudaFree(b->d_fhat_off);
   cudaFree(b->d_counter);
@@ -308,6 +367,22 @@ static int batch_autotune(Batch *b, int reps)
           const float ms = time_b_pair(t, reps);
           if (ms < best.ms) best = {T, tpn, ms};
         }
+        batch_free(t);
+      }
+      // the column kernels on the plans' own 32^2 tiles keyed by column
+      bool col_ok = true;
+      for (auto *p : sample) {
+        plan_retile_f(p, 0);
+        PlanViewF v;
+        plan_view_f(p, &v);
+        col_ok = col_ok && v.col2;
+      }
+      if (col_ok) {
+        Batch *t = batch_new(sample.data(), (int)sample.size());
+        for (auto &P : t->host_plans) P.tpn = 0;
+        batch_tables(t);
+        const float ms = time_b_pair(t, reps);
+        if (ms < best.ms) best = {0, 0, ms};
         batch_free(t);
       }
       hit = g_tune.insert({cl.first, best}).first;
@@ -388,6 +463,25 @@ long long nfftf_gb_batch_nodes(void *batch) { return reinterpret_cast<Batch *>(b
 int nfftf_gb_batch_items(void *batch) { return reinterpret_cast<Batch *>(batch)->nitems; }
 
 // chosen (T, tpn) of plan k (after autotuning)
+int nfftf_gb_batch_set_config(void *batch, int k, int T, int tpn)
+{
+  Batch *b = reinterpret_cast<Batch *>(batch);
+  if (!b || k < 0 || k >= (int)b->plans.size()) return -1;
+  if (tpn == 0) {
+    if (T != 32) return -1;
+    plan_retile_f(b->plans[k], 0);
+    PlanViewF v;
+    plan_view_f(b->plans[k], &v);
+    if (!v.col2) return -1;
+  } else {
+    if ((T != 8 && T != 16 && T != 32) || (tpn != 1 && tpn != 4 && tpn != 16)) return -1;
+    plan_retile_f(b->plans[k], T);
+  }
+  b->host_plans[k].tpn = tpn;
+  batch_tables(b);
+  return 0;
+}
+
 int nfftf_gb_batch_plan_config(void *batch, int k, int *T, int *tpn)
 {
   Batch *b = reinterpret_cast<Batch *>(batch);

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/nfft_gb300.h"
+#include "gb_col2.cuh"
 #include "gb_internal.h"
 
 namespace gb {
@@ -35,8 +36,9 @@ struct BPlan {
   float2 *grid;           // this plan's grid in the batch arena
   long long grid_off;     // offset of grid in the arena (complex elements)
   long long fhat_off;     // offset of this plan in the concatenated f_hat index space
-  int tpn;                // threads per node of the B / B^T kernels (1, 4, 16)
+  int tpn;                // threads per node of the B / B^T kernels (1, 4, 16); 0: column kernels
   int pad;
+  const WinPoly *poly;    // the plan's polynomial window (device copy; column kernels)
 };
 
 struct BItem {
@@ -287,4 +289,52 @@ __global__ void __launch_bounds__(BT_THREADS) k_batch_bt2(const BPlan *__restric
   }
 }
 
+// Persistent column B / B^T (gb_col2.cuh) over the items of the plans in
+// column mode: the same queue discipline, one work item per CTA pass.
+#define GB_C2_DISPATCH(FN, ...)          \
+  switch (P.g.w) {                       \
+    case 10: FN<10>(__VA_ARGS__); break; \
+    case 14: FN<14>(__VA_ARGS__); break; \
+    default: break;                      \
+  }
+
+__global__ void __launch_bounds__(C2_THREADS, 2) k_batch_b2c(const BPlan *__restrict__ plans,
+                                                              const BItem *__restrict__ items, int nitems,
+                                                              int *__restrict__ counter)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int k = s_item;
+    if (k >= nitems) break;
+    const BItem bi = items[k];
+    const BPlan &P = plans[bi.plan];
+    const WorkItem it = {bi.tile, bi.start, bi.end, 0};
+    GB_C2_DISPATCH(c2_b_item, it, P.grid, P.xs, P.perm, P.f_out, P.g, *P.poly, smem_raw)
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(C2_THREADS, 2) k_batch_bt2c(const BPlan *__restrict__ plans,
+                                                               const BItem *__restrict__ items, int nitems,
+                                                               int *__restrict__ counter)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int k = s_item;
+    if (k >= nitems) break;
+    const BItem bi = items[k];
+    const BPlan &P = plans[bi.plan];
+    const WorkItem it = {bi.tile, bi.start, bi.end, 0};
+    GB_C2_DISPATCH(c2_bt_item, it, P.grid, P.xs, P.perm, P.f_in, P.g, *P.poly, smem_raw)
+    __syncthreads();
+  }
+}
+
 }  // namespace gb
+

@@ -125,10 +125,13 @@ struct PlanViewF {
   float2 *fhat;
   float2 *f;
   bool tiled, group3, direct, ready;
+  bool col2;           // nodes keyed by 2-D column (the column kernels apply)
+  const WinPoly *poly; // the plan's polynomial window (host copy)
   cudaStream_t stream;
 };
 bool plan_view_f(void *nfftf_plan_ptr, PlanViewF *v);
-// re-bin a 2-D plan's nodes on tiles of edge T (8, 16 or 32)
+// re-bin a 2-D plan's nodes on tiles of edge T (8, 16 or 32), or with T = 0
+// as the plan would by itself (32^2 tiles keyed by column where it can)
 void plan_retile_f(void *nfftf_plan_ptr, int T);
 
 // ---------------------------------------------------------------- NDFT

@@ -1089,6 +1089,8 @@ bool plan_view_f(void *pp, PlanViewF *v)
   v->group3 = c->group3;
   v->direct = c->direct;
   v->ready = c->nodes_ready;
+  v->col2 = c->col2;
+  v->poly = &c->poly;
   v->stream = c->stream;
   return true;
 }

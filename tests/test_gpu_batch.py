@@ -29,15 +29,22 @@ def _single_results(plans, data, seed):
     return refs
 
 
-@pytest.mark.parametrize("autotune", [False, True])
+@pytest.mark.parametrize("autotune", [False, True, "column", "mixed"])
 def test_batch_matches_single_plans(gpulib, autotune):
     plans, data = batch.random_plans(gpulib, 24, seed=3, sizes=(32, 64), mmin=300, mmax=5000)
     refs = _single_results(plans, data, 3)
     b = batch.Batch(gpulib, plans)
-    if autotune:
+    if autotune in ("column", "mixed"):
+        # every plan (or every other one) on the column kernels, the rest per node
+        for k in range(len(plans)):
+            cfg = (32, 0) if autotune == "column" or k % 2 == 0 else (16, 4)
+            assert b.set_config(k, *cfg) == 0
+            assert b.config(k) == cfg
+        assert b.set_config(0, 8, 0) == -1
+    elif autotune:
         assert b.autotune(reps=2) >= 1
         cfgs = {b.config(k) for k in range(len(plans))}
-        assert all(T in (8, 16, 32) and t in (1, 4, 16) for T, t in cfgs)
+        assert all((T in (8, 16, 32) and t in (1, 4, 16)) or (T, t) == (32, 0) for T, t in cfgs)
     put, get = batch.device_io(gpulib)
     for p, (fh, f, *_r) in zip(plans, refs):
         put(p, "f_hat", fh)

@@ -299,6 +299,7 @@ struct SolverState {
   int refresh_every = 0;
   long long iter = 0;
   nfft_plan *plan64 = nullptr;
+  cudaEvent_t refresh_ev = nullptr;  // orders the refresh's FP64 stream against the solver's
   // CUDA graph of one step's launches (steepest descent, CGNR, CGNE)
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
@@ -388,8 +389,8 @@ void refresh_residual<float>(SolverState<float> *st)
   double2 *qfh = (double2 *)nfft_gb_device_f_hat(q);
   double2 *qf = (double2 *)nfft_gb_device_f(q);
   cudaStream_t qs = (cudaStream_t)nfft_gb_get_stream(q);
-  cudaEvent_t e;
-  GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (!st->refresh_ev) GB_CUDA(cudaEventCreateWithFlags(&st->refresh_ev, cudaEventDisableTiming));
+  cudaEvent_t e = st->refresh_ev;
   GB_CUDA(cudaEventRecord(e, st->s));
   GB_CUDA(cudaStreamWaitEvent(qs, e, 0));
   k_f32_to_f64<<<grid_for(st->N), 256, 0, qs>>>(st->fh, qfh, st->N);
@@ -399,7 +400,6 @@ void refresh_residual<float>(SolverState<float> *st)
   GB_LAUNCHED("residual_f64");
   GB_CUDA(cudaEventRecord(e, qs));
   GB_CUDA(cudaStreamWaitEvent(st->s, e, 0));
-  GB_CUDA(cudaEventDestroy(e));
 }
 
 template <typename R>
@@ -781,6 +781,7 @@ static void finalize_solver(typename SApi<R>::splan *ths)
   if (st) {
     cudaStreamSynchronize(st->s);
     if (st->gexec) cudaGraphExecDestroy(st->gexec);
+    if (st->refresh_ev) cudaEventDestroy(st->refresh_ev);
     cudaFree(st->y);
     cudaFree(st->r);
     cudaFree(st->v);

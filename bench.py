@@ -247,6 +247,25 @@ def accuracy_sample(lib, wl, x, fh_host, f_host, f_out, n_trafo=256, n_adj=1024)
             "adjoint_rel_l2_vs_ndft": e_a, "adjoint_subset_nodes": n_adj}
 
 
+def max_over_ranks(v, dist=None, device="cpu"):
+    """The largest of the ranks' values v (v itself on one rank): a replica
+    run is as slow as its slowest rank."""
+    if dist is None:
+        return float(v)
+    import torch
+    t = torch.tensor([float(v)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(ms_total, nodes_per_rank, steps, dist=None, device="cpu"):
+    """Whole-job rate of replicas (each rank transforms its own nodes, no data
+    exchange): (ms per step from the slowest rank, nodes of all ranks / s)."""
+    world = dist.get_world_size() if dist is not None else 1
+    ms_step = max_over_ranks(ms_total, dist, device) / steps
+    return ms_step, nodes_per_rank * world / (ms_step * 1e-3)
+
+
 def run_gpu(args, wl):
     import torch
     import nfft_gb300
@@ -328,14 +347,9 @@ def run_gpu(args, wl):
     sums = (C.c_float * 7)()
     counts = (C.c_int * 2)()
     end(pa, sums, counts)
-    # trafo: k_d_pad + k_b3_cell; adjoint: k_gather_c + k_bt3_col + k_d_crop (cuFFT not counted)
-    launches = 5 * args.steps
-    if dist is not None:
-        t = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    value = M * world / (ms_step * 1e-3)
+    # trafo: k_d_pad + k_b3_cell; adjoint: k_bt3_col + k_d_crop (cuFFT and memsets not counted)
+    launches = 4 * args.steps
+    ms_step, value = replica_rate(ms_total, M, args.steps, dist, dev)
 
     # ---- accuracy of this very run against the FP64 NDFT (on the GPU)
     accuracy = None
@@ -353,11 +367,7 @@ def run_gpu(args, wl):
         t1 = time.perf_counter()
         if it >= args.warmup:
             e2e_times.append(t1 - t0)
-    e2e_s = sum(e2e_times) / len(e2e_times)
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), dist, dev)
     e2e_value = M * world / e2e_s
     h2d = NN * 8 + M * 8
     d2h = M * 8 + NN * 8

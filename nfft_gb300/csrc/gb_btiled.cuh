@@ -255,10 +255,7 @@ static void run_bt(const WorkItem *items, int nitems, typename Cx<R>::T *grid, c
   GB_LAUNCHED("bt_tiled");
 }
 
-#define GB_CASE_B(D, W) \
-  case D * 1000 + W: run_b<R, D, W>(items, nitems, grid, xs, perm, f, g, s); return;
-#define GB_CASE_BT(D, W) \
-  case D * 1000 + W: run_bt<R, D, W>(items, nitems, grid, xs, perm, f, g, s); return;
+#define GB_TILED_W(X) X(6) X(8) X(10) X(12) X(14) X(16) X(18)
 #define GB_CASE_OK(D, W) case D * 1000 + W:
 
 template <typename R>
@@ -274,16 +271,58 @@ bool tiled_supported_impl(int d, int w)
   }
 }
 
+// One dimension's kernels, by window width (instantiated per precision and
+// dimension in gb_btiled_<precision><d>.cu, which compile in parallel).
+template <typename R, int D>
+void launch_b_tiled_dim(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
+                        const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+{
+  switch (g.w) {
+#define GB_CASE_BW(W) \
+  case W: run_b<R, D, W>(items, nitems, grid, xs, perm, f, g, s); return;
+    GB_TILED_W(GB_CASE_BW)
+#undef GB_CASE_BW
+    default:
+      fatal("no tiled interpolation kernel for d=%d w=%d", g.d, g.w);
+  }
+}
+
+template <typename R, int D>
+void launch_bt_tiled_dim(const WorkItem *items, int nitems, typename Cx<R>::T *grid, const R *xs,
+                         const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
+{
+  switch (g.w) {
+#define GB_CASE_BTW(W) \
+  case W: run_bt<R, D, W>(items, nitems, grid, xs, perm, f, g, s); return;
+    GB_TILED_W(GB_CASE_BTW)
+#undef GB_CASE_BTW
+    default:
+      fatal("no tiled spreading kernel for d=%d w=%d", g.d, g.w);
+  }
+}
+
+#define GB_TILED_DIM_DECL(EXT, R, D)                                                                        \
+  EXT template void launch_b_tiled_dim<R, D>(const WorkItem *, int, const Cx<R>::T *, const R *,         \
+                                             const uint32_t *, Cx<R>::T *, const Geom<R> &, cudaStream_t); \
+  EXT template void launch_bt_tiled_dim<R, D>(const WorkItem *, int, Cx<R>::T *, const R *,              \
+                                              const uint32_t *, const Cx<R>::T *, const Geom<R> &, cudaStream_t);
+GB_TILED_DIM_DECL(extern, float, 1)
+GB_TILED_DIM_DECL(extern, float, 2)
+GB_TILED_DIM_DECL(extern, float, 3)
+GB_TILED_DIM_DECL(extern, double, 1)
+GB_TILED_DIM_DECL(extern, double, 2)
+GB_TILED_DIM_DECL(extern, double, 3)
+
 template <typename R>
 void launch_b_tiled_impl(const WorkItem *items, int nitems, const typename Cx<R>::T *grid,
                          const R *xs, const uint32_t *perm, typename Cx<R>::T *f,
                          const Geom<R> &g, cudaStream_t s)
 {
   if (nitems <= 0) return;
-  switch (g.d * 1000 + g.w) {
-    GB_TILED_WIDTHS(GB_CASE_B, 1)
-    GB_TILED_WIDTHS(GB_CASE_B, 2)
-    GB_TILED_WIDTHS(GB_CASE_B, 3)
+  switch (g.d) {
+    case 1: launch_b_tiled_dim<R, 1>(items, nitems, grid, xs, perm, f, g, s); return;
+    case 2: launch_b_tiled_dim<R, 2>(items, nitems, grid, xs, perm, f, g, s); return;
+    case 3: launch_b_tiled_dim<R, 3>(items, nitems, grid, xs, perm, f, g, s); return;
     default:
       fatal("no tiled interpolation kernel for d=%d w=%d", g.d, g.w);
   }
@@ -295,10 +334,10 @@ void launch_bt_tiled_impl(const WorkItem *items, int nitems, typename Cx<R>::T *
                           const Geom<R> &g, cudaStream_t s)
 {
   if (nitems <= 0) return;
-  switch (g.d * 1000 + g.w) {
-    GB_TILED_WIDTHS(GB_CASE_BT, 1)
-    GB_TILED_WIDTHS(GB_CASE_BT, 2)
-    GB_TILED_WIDTHS(GB_CASE_BT, 3)
+  switch (g.d) {
+    case 1: launch_bt_tiled_dim<R, 1>(items, nitems, grid, xs, perm, f, g, s); return;
+    case 2: launch_bt_tiled_dim<R, 2>(items, nitems, grid, xs, perm, f, g, s); return;
+    case 3: launch_bt_tiled_dim<R, 3>(items, nitems, grid, xs, perm, f, g, s); return;
     default:
       fatal("no tiled spreading kernel for d=%d w=%d", g.d, g.w);
   }

@@ -8,7 +8,7 @@ namespace gb {
 
 // per-plan kernels: one CTA per work item
 template <int W>
-__global__ void __launch_bounds__(C2_THREADS, 2) k_bt2_col(const WorkItem *__restrict__ items,
+__global__ void __launch_bounds__(C2_THREADS, 3) k_bt2_col(const WorkItem *__restrict__ items,
                                                             float2 *__restrict__ grid,
                                                             const float *__restrict__ xs,
                                                             const uint32_t *__restrict__ perm,

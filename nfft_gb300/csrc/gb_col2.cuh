@@ -59,7 +59,7 @@ struct C2 {
   static constexpr int EXT = C2_TILE + W - 1;  // padded subgrid edge
   static constexpr int SY = EXT | 1;           // subgrid row stride (complex)
   // per-warp scratch (floats): x vectors (complex for B^T, real for B), y vectors
-  static constexpr int WARP_FLOATS_T = 2 * XS * C2_CHUNK + YS * C2_CHUNK;
+  static constexpr int WARP_FLOATS_T = XS * C2_CHUNK + YS * C2_CHUNK;  // B^T keeps f_j at y slot YV
   static constexpr int WARP_FLOATS_B = XS * C2_CHUNK + YS * C2_CHUNK;
   static_assert(ROWS <= 16, "a column's rows fill at most a half-warp");
   static_assert(4 * HP >= NPOS, "two halves cover the column's y positions");
@@ -148,18 +148,11 @@ __device__ __forceinline__ int c2_setup(const float *x, const Geom<float> &g, in
   const int ox = ux % P::CX, oy = uy % C2_CY;
   float v[W];
   kb_poly_taps_s<W>(s0, poly.c[0], v);
-  if (ADJ) {
-    float2 *xc = reinterpret_cast<float2 *>(xv);
 #pragma unroll
-    for (int q = 0; q < 16; ++q) xc[q] = make_float2(0.f, 0.f);
+  for (int q = 0; q < 16; ++q) xv[q] = 0.f;
 #pragma unroll
-    for (int l = 0; l < W; ++l) xc[ox + l] = make_float2(v[l] * fj.x, v[l] * fj.y);
-  } else {
-#pragma unroll
-    for (int q = 0; q < 16; ++q) xv[q] = 0.f;
-#pragma unroll
-    for (int l = 0; l < W; ++l) xv[ox + l] = v[l];
-  }
+  for (int l = 0; l < W; ++l) xv[ox + l] = v[l];
+  if (ADJ) reinterpret_cast<float2 *>(yv)[P::YV / 2] = fj;  // the node's f_j beside its y taps
 #pragma unroll
   for (int q = 0; q < P::YV / 2; ++q) reinterpret_cast<float2 *>(yv)[q] = make_float2(0.f, 0.f);
   kb_poly_taps_s<W>(s1, poly.c[1], v);
@@ -180,8 +173,8 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
   constexpr int CX = P::CX, HP = P::HP, SY = P::SY;
   float *const base = reinterpret_cast<float *>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *const wx = base + warp * P::WARP_FLOATS_T;  // complex, stride XS
-  float *const wy = wx + 2 * P::XS * C2_CHUNK;
+  float *const wx = base + warp * P::WARP_FLOATS_T;  // real, stride XS
+  float *const wy = wx + P::XS * C2_CHUNK;
   float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_T);
 
   const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
@@ -195,12 +188,12 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
     int col = -1;
     if (lane < np)
       col = c2_setup<W, true>(xs + 2LL * (a + lane), g, org0, org1, poly, f[perm[a + lane]],
-                              wx + 2 * P::XS * lane, wy + P::YS * lane);
+                              wx + P::XS * lane, wy + P::YS * lane);
     // the task's nodes are in column order: runs of one column
     const int prevc = __shfl_up_sync(0xffffffffu, col, 1);
     unsigned starts = __ballot_sync(0xffffffffu, lane < np && (lane == 0 || col != prevc));
     __syncwarp();
-    const float2 *xrow = reinterpret_cast<const float2 *>(wx) + r;
+    const float *xrow = wx + r;
     const float2 *ypair = reinterpret_cast<const float2 *>(wy) + h * HP;
     while (starts) {
       const int s = __ffs(starts) - 1;
@@ -213,8 +206,10 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
       for (int q = 0; q < HP; ++q) ar[q] = ai[q] = make_float2(0.f, 0.f);
 #pragma unroll 2
       for (int j = s; j < e; ++j) {
-        const float2 xf = xrow[j * P::XS];
-        const float2 hr = make_float2(xf.x, xf.x), hi = make_float2(xf.y, xf.y);
+        const float xw = xrow[j * P::XS];
+        const float2 fj = reinterpret_cast<const float2 *>(wy + j * P::YS)[P::YV / 2];
+        const float xr = xw * fj.x, xi = xw * fj.y;
+        const float2 hr = make_float2(xr, xr), hi = make_float2(xi, xi);
         const float2 *yp = ypair + j * (P::YS / 2);
 #pragma unroll
         for (int q = 0; q < HP; ++q) {

@@ -317,7 +317,7 @@ class TrigPlan:
     precompute_one_psi, fill f_hat (real, N_total) or f, trafo / adjoint or
     their _direct forms."""
 
-    def __init__(self, lib, kind, single, N, M, n, m, flags, fftw_flags=None):
+    def __init__(self, lib, kind, single, N, M, n=None, m=None, flags=None, fftw_flags=None):
         self.lib = lib
         self.pfx = kind + ("f_" if single else "_")
         self.dt = np.float32 if single else np.float64
@@ -326,13 +326,19 @@ class TrigPlan:
         self.M = int(M)
         if fftw_flags is None:
             fftw_flags = abi.FFTW_ESTIMATE | abi.FFTW_DESTROY_INPUT
-        fn = getattr(lib, self.pfx + "init_guru")
-        fn.restype = None
-        fn.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
-                       C.c_uint, C.c_uint]
         Nc = (C.c_int * self.d)(*[int(v) for v in N])
-        nc = (C.c_int * self.d)(*[int(v) for v in n])
-        fn(C.addressof(self.p), self.d, Nc, self.M, nc, int(m), int(flags), int(fftw_flags))
+        if n is None:  # the reference's defaults (X(init): n, m and flags chosen by the library)
+            fn = getattr(lib, self.pfx + "init")
+            fn.restype = None
+            fn.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+            fn(C.addressof(self.p), self.d, Nc, self.M)
+        else:
+            fn = getattr(lib, self.pfx + "init_guru")
+            fn.restype = None
+            fn.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
+                           C.c_uint, C.c_uint]
+            nc = (C.c_int * self.d)(*[int(v) for v in n])
+            fn(C.addressof(self.p), self.d, Nc, self.M, nc, int(m), int(flags), int(fftw_flags))
         self.N_total = int(self.p.N_total)
         self.x = _view(self.p.x, self.M * self.d, self.dt)
         self.f = _view(self.p.f, self.M, self.dt)

@@ -7,6 +7,8 @@
   (tests/golden/refrun.npz, made by tests/golden/make_golden.py): transforms,
   sorted index_x bit-exactly, D coefficients, and CGNR / CGNE iterates.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -110,6 +112,17 @@ def test_oracle_bessel_i0():
     for x in [0.0, 1.0, 2.5, 10.0, 37.7, 60.0, 150.0]:
         ref = float(scipy_special.i0(x))
         assert abs(oracle.bessel_i0(x) - ref) <= 8 * np.finfo(float).eps * ref
+
+
+def test_oracle_bessel_i0_reference_table():
+    """The oracle's I0 against the reference's own table (tests/bessel.c:29-139,
+    I0(j) at j = 0, 1, 2, ...) within the reference test's bound of 4 eps
+    relative (tests/bessel.c:141-167)."""
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bessel_i0.npz"))
+    assert len(z["i0"]) > 50
+    bound = 4 * np.finfo(float).eps
+    for x, ref in zip(z["x"], z["i0"]):
+        assert abs(oracle.bessel_i0(float(x)) - ref) <= bound * ref, (x, oracle.bessel_i0(float(x)), ref)
 
 
 def test_oracle_sort_is_stable_and_keyed():

@@ -146,6 +146,28 @@ def _util(name, restype, argtypes):
 def test_next_power_of_2_semantics():
     f = _util("nfft_next_power_of_2", C.c_ssize_t, [C.c_ssize_t])
     assert [f(v) for v in (-3, 0, 1, 2, 3, 4, 5, 255, 256, 257)] == [-1, 1, 2, 2, 4, 4, 8, 256, 256, 512]
+
+    def by_halving(N):
+        # the reference test's loop (tests/util.c:85-113): the smallest power
+        # of two >= N, 1 for N = 0 and 2 for N = 1
+        if N == 1:
+            return 2
+        n, logn, odd = N, 0, False
+        while n != 1:
+            odd = odd or n % 2 == 1
+            n //= 2
+            logn += 1
+        if not odd:
+            logn -= 1
+        for _ in range(logn + 1):
+            n *= 2
+        return n
+    # powers of two and one less, as tests/util.c:116-153 (64-bit index)
+    for i in range(62):
+        j = 1 << i
+        assert f(j) == by_halving(j), j
+        if j > 1:
+            assert f(j - 1) == by_halving(j - 1), j - 1
     assert _util("nfft_exp2i", C.c_ssize_t, [C.c_ssize_t])(10) == 1024
 
 

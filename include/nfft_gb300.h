@@ -79,7 +79,12 @@ void *X(gb_device_y)(X(plan_complex) *ths); \
 /* 1 (default): steepest descent, CGNR and CGNE steps replay a CUDA graph of \
  * the step's launches, captured on first use and again after the plan's \
  * nodes change; 0: launch them one by one.  The results are the same. */ \
-int X(gb_set_graphs)(X(plan_complex) *ths, int on);
+int X(gb_set_graphs)(X(plan_complex) *ths, int on); \
+/* k calls of loop_one_step without a host round trip in between: the steps \
+ * are enqueued back to back and the host struct is updated once at the end \
+ * (as after the k-th call); dot_r_hist (host, k doubles, or NULL) receives \
+ * dot_r_iter after each step. */ \
+int X(gb_loop_steps)(X(plan_complex) *ths, int k, double *dot_r_hist);
 
 NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_DOUBLE)
 NFFTGB_DEFINE_SOLVER_API(SOLVER_MANGLE_FLOAT)

@@ -300,6 +300,8 @@ struct SolverState {
   long long iter = 0;
   nfft_plan *plan64 = nullptr;
   cudaEvent_t refresh_ev = nullptr;  // orders the refresh's FP64 stream against the solver's
+  double *hist = nullptr;  // dot_r of each step of a multi-step call
+  int hist_cap = 0;
   // CUDA graph of one step's launches (steepest descent, CGNR, CGNE)
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
@@ -548,7 +550,7 @@ static void enqueue_step(SolverState<R> *st, bool refresh)
 }
 
 template <typename R>
-static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
+static void dev_step_enqueue(typename SApi<R>::splan *ths, SolverState<R> *st)
 {
   typedef typename Cx<R>::T C;
   const long long M = st->M, N = st->N;
@@ -591,7 +593,37 @@ static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
   } else {
     enqueue_step<R>(st, refresh);
   }
+}
+
+template <typename R>
+static void dev_step(typename SApi<R>::splan *ths, SolverState<R> *st)
+{
+  dev_step_enqueue<R>(ths, st);
   publish<R>(ths, st, false);
+}
+
+// k steps enqueued back to back (no host round trip between them), then one
+// publish; dot_r of every step lands in dot_r_hist (host, k values) when
+// given.  Landweber takes its step size from the host struct, which does not
+// change in between.
+template <typename R>
+static int dev_steps(typename SApi<R>::splan *ths, SolverState<R> *st, int k, double *dot_r_hist)
+{
+  if (k <= 0) return 0;
+  if (dot_r_hist && st->hist_cap < k) {
+    if (st->hist) GB_CUDA(cudaFree(st->hist));
+    GB_CUDA(cudaMalloc(&st->hist, (size_t)k * sizeof(double)));
+    st->hist_cap = k;
+  }
+  for (int i = 0; i < k; ++i) {
+    dev_step_enqueue<R>(ths, st);
+    if (dot_r_hist)
+      GB_CUDA(cudaMemcpyAsync(st->hist + i, st->scal + S_DOT_R, sizeof(double), cudaMemcpyDeviceToDevice, st->s));
+  }
+  if (dot_r_hist)
+    GB_CUDA(cudaMemcpyAsync(dot_r_hist, st->hist, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, st->s));
+  publish<R>(ths, st, false);
+  return 0;
 }
 
 // ---------------------------------------------------------------- host path
@@ -782,6 +814,7 @@ static void finalize_solver(typename SApi<R>::splan *ths)
     cudaStreamSynchronize(st->s);
     if (st->gexec) cudaGraphExecDestroy(st->gexec);
     if (st->refresh_ev) cudaEventDestroy(st->refresh_ev);
+    if (st->hist) cudaFree(st->hist);
     cudaFree(st->y);
     cudaFree(st->r);
     cudaFree(st->v);
@@ -874,6 +907,12 @@ extern "C" {
   {                                                                                             \
     SolverState<R> *st = state_of<R>(ths);                                                      \
     return st ? (void *)st->y : nullptr;                                                        \
+  }                                                                                             \
+  int X##gb_loop_steps(X##plan_complex *ths, int k, double *dot_r_hist)                          \
+  {                                                                                             \
+    SolverState<R> *st = state_of<R>(ths);                                                      \
+    if (!st) return -1;                                                                         \
+    return dev_steps<R>(ths, st, k, dot_r_hist);                                                \
   }                                                                                             \
   int X##gb_set_graphs(X##plan_complex *ths, int on)                                            \
   {                                                                                             \

@@ -1,8 +1,8 @@
 """Inverse NFFT (CGNR) driver on the GPU library, for benchmarks and tests.
 
 Runs the solver through the reference-facing C ABI (solver_* over nfft_*
-plans, solverf_* over nfftf_* plans) with the library's extensions: scalars-
-only synchronisation inside the timed loop, and an FP64 residual refresh for
+plans, solverf_* over nfftf_* plans) with the library's extensions: timed
+steps enqueued back to back (solver_gb_loop_steps), and an FP64 residual refresh for
 single-precision solvers (r = y - A f recomputed by an FP64 transform every
 `refresh` iterations, kernel/solver/solver.c:81-125 being the formula).
 """
@@ -49,6 +49,8 @@ class CGNR:
         self._set_sync = _ext(lib, pfx + "gb_set_sync", C.c_int, [C.c_void_p, C.c_int])
         self._sync = _ext(lib, pfx + "gb_sync", C.c_int, [C.c_void_p])
         self._refresh = _ext(lib, pfx + "gb_set_refresh", C.c_int, [C.c_void_p, C.c_int])
+        self._steps = _ext(lib, pfx + "gb_loop_steps", C.c_int,
+                           [C.c_void_p, C.c_int, C.POINTER(C.c_double)])
         self.addr = C.addressof(self.solver.s)
         if refresh:
             self._refresh(self.addr, int(refresh))
@@ -64,6 +66,14 @@ class CGNR:
 
     def step(self):
         self.solver.loop_one_step()
+
+    def steps(self, k):
+        """k steps enqueued back to back (one host synchronisation at the
+        end); returns dot_r after each step."""
+        hist = np.zeros(k, dtype=np.float64)
+        if k > 0:
+            self._steps(self.addr, int(k), hist.ctypes.data_as(C.POINTER(C.c_double)))
+        return hist
 
     @property
     def f_hat(self):
@@ -99,16 +109,14 @@ def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14):
 
 
 def run_iterations(lib, single, N, x, m, y, iters, w=None, refresh=0):
-    """Run `iters` CGNR steps timed (scalars-only synchronisation per step);
-    returns (f_hat_iter after the last step, seconds, per-step dot_r)."""
+    """Run `iters` CGNR steps timed (enqueued back to back, one host
+    synchronisation); returns (f_hat_iter after the last step, seconds,
+    per-step dot_r)."""
     s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0)
     s.set_sync(0)
-    dots = []
     t0 = time.perf_counter()
     s.before_loop()
-    for _ in range(iters):
-        s.step()
-        dots.append(s.dot_r)
+    dots = list(s.steps(iters))
     s.sync()
     t1 = time.perf_counter()
     out = s.f_hat.copy()
@@ -126,7 +134,7 @@ def time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, w=None, refresh=
                           reference's own stopping rule is on its residual,
                           applications/mri/mri2d/reconstruct_data_2d.c:123-131).
     A first untimed run finds the iteration count; a second run of exactly
-    that many iterations is timed (scalars-only synchronisation per step, the
+    that many iterations is timed (the steps enqueued back to back, the
     iterate copied back once at the end).  Returns dict(iters, seconds, err,
     reached) with err the criterion's value at the end of the timed run."""
     def measure(s):
@@ -150,8 +158,7 @@ def time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=1e-5, w=None, refresh=
     s.set_sync(0)
     t0 = time.perf_counter()
     s.before_loop()
-    for _ in range(k):
-        s.step()
+    s.steps(k)
     s.sync()
     t1 = time.perf_counter()
     err2 = measure(s)

@@ -181,3 +181,34 @@ def test_graph_steps_match_launched_steps(gpulib, single, flags):
         assert rel_l2(fa, fb) < tol, (it, rel_l2(fa, fb))
         for a, b in zip(sa, sb):
             assert abs(a - b) <= 10 * tol * abs(b) + 1e-30, (it, a, b)
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_multi_step_call_matches_single_steps(gpulib, single):
+    """solver[f]_gb_loop_steps(k) leaves the iterate and scalars of k
+    loop_one_step calls (to rounding: the adjoint's atomic accumulation) and
+    reports dot_r of every step."""
+    from nfft_gb300 import infft
+    N, M, m = [32, 32], 2500, 6
+    x, _, y = seeded_case(N, M, seed=23)
+    dt = np.float32 if single else np.float64
+    a = infft.CGNR(gpulib, single, N, x.astype(dt), m, y, refresh=3 if single else 0)
+    a.set_sync(2)
+    a.before_loop()
+    dots = []
+    for _ in range(7):
+        a.step()
+        dots.append(a.dot_r)
+    fa = a.f_hat.copy()
+    a.close()
+    b = infft.CGNR(gpulib, single, N, x.astype(dt), m, y, refresh=3 if single else 0)
+    b.set_sync(2)
+    b.before_loop()
+    hist = b.steps(7)
+    fb = b.f_hat.copy()
+    db = b.dot_r
+    b.close()
+    tol = 1e-4 if single else 1e-11
+    assert rel_l2(fb, fa) < tol
+    assert np.allclose(hist, dots, rtol=10 * tol)
+    assert abs(db - dots[-1]) <= 10 * tol * abs(dots[-1])

@@ -1,5 +1,6 @@
 """The reference's own single-precision error at the 3-D benchmark shape
-(N = 128^3, n = 256^3, m = 4, Kaiser-Bessel): nfftf_trafo and nfftf_adjoint
+(N = 128^3, n = 256^3, m = 4, Kaiser-Bessel), and at the 2-D radial shape of
+the inverse-NFFT workload (N = 256^2, n = 512^2, m = 6): nfftf_trafo and nfftf_adjoint
 of the reference compiled in place (oracle/ref/Makefile, single-precision
 FFT stand-in) on a 4096-node subset plan with seeded inputs, stored as
 tests/golden/cfg2_single_ref.npz: the trafo output at all 4096 nodes and the
@@ -25,6 +26,9 @@ from nfft_gb300.plan import Plan  # noqa: E402
 N, n, m, M, SEED, NSAMP = [128, 128, 128], [256, 256, 256], 4, 4096, 2024, 4096
 FLAGS = (abi.PRE_PHI_HUT | abi.PRE_PSI | abi.MALLOC_X | abi.MALLOC_F_HAT | abi.MALLOC_F | abi.FFTW_INIT
          | abi.FFT_OUT_OF_PLACE)
+# the 2-D radial shape of the inverse-NFFT workload: every 50th node of the
+# 402 x 512 radial lines (the first 4096), N = 256^2, n = 512^2, m = 6
+N2, n2, m2 = [256, 256], [512, 512], 6
 
 
 def inputs():
@@ -39,10 +43,38 @@ def inputs():
     return x, fh, f, idx
 
 
+def inputs_radial():
+    """The same for the 2-D radial shape."""
+    from nfft_gb300 import workloads
+    x = workloads.radial_nodes(402, 512)[::50][:M].astype(np.float32)
+    rng = np.random.default_rng(SEED + 1)
+    NN = int(np.prod(N2))
+    fh = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
+    idx = np.sort(rng.choice(NN, NSAMP, replace=False))
+    return x, fh, f, idx
+
+
+def run(lib, single, Nc, nc, mc, x, fh, f, idx):
+    p = Plan(lib, single, Nc, len(x), n=nc, m=mc, flags=FLAGS)
+    p.x[:] = x
+    p.precompute_one_psi()
+    p.f_hat[:] = fh
+    p.trafo()
+    out_f = p.f.copy()
+    p.f[:] = f
+    p.adjoint()
+    out_fh = p.f_hat[idx].copy()
+    p.finalize()
+    return out_f, out_fh
+
+
 def main():
     ref = oracle.load_reference(True)
     if ref is None:
         sys.exit("reference library not built (oracle.build_reference())")
+    x2, fh2, f2, idx2 = inputs_radial()
+    f_ref2, fhat_ref2 = run(ref, True, N2, n2, m2, x2, fh2, f2, idx2)
     x, fh, f, idx = inputs()
     p = Plan(ref, True, N, M, n=n, m=m, flags=FLAGS)
     p.x[:] = x
@@ -54,7 +86,8 @@ def main():
     p.adjoint()
     fhat_ref = p.f_hat[idx].copy()
     p.finalize()
-    np.savez_compressed(os.path.join(HERE, "cfg2_single_ref.npz"), f_ref=f_ref, fhat_ref=fhat_ref, idx=idx)
+    np.savez_compressed(os.path.join(HERE, "cfg2_single_ref.npz"), f_ref=f_ref, fhat_ref=fhat_ref, idx=idx,
+                        radial_f_ref=f_ref2, radial_fhat_ref=fhat_ref2, radial_idx=idx2)
     print("cfg2_single_ref.npz written")
 
 

@@ -1,5 +1,6 @@
 """The single-precision error at the 3-D benchmark shape (N = 128^3,
-n = 256^3, m = 4), held to at most twice the reference's own nfftf error on
+n = 256^3, m = 4) and at the 2-D radial inverse-NFFT shape, held to at most
+twice the reference's own nfftf error on
 the same problem: a 4096-node subset plan with seeded inputs, the reference's
 nfftf_trafo / nfftf_adjoint outputs from tests/golden/cfg2_single_ref.npz
 (tests/golden/make_cfg2_single_ref.py), the FP64 NDFT (nfft_trafo_direct /
@@ -52,6 +53,30 @@ def test_fp32_error_within_twice_the_reference_nfftf(gpulib):
     e_ref_t, e_gpu_t = rel(z["f_ref"], f_ndft), rel(f_gpu, f_ndft)
     e_ref_a, e_gpu_a = rel(z["fhat_ref"], fhat_ndft), rel(fhat_gpu, fhat_ndft)
     print("trafo: reference nfftf %.2e, this library %.2e; adjoint: reference %.2e, this library %.2e"
+          % (e_ref_t, e_gpu_t, e_ref_a, e_gpu_a))
+    assert e_gpu_t <= 2 * e_ref_t, (e_gpu_t, e_ref_t)
+    assert e_gpu_a <= 2 * e_ref_a, (e_gpu_a, e_ref_a)
+
+
+def test_fp32_error_radial_2d_within_twice_the_reference_nfftf(gpulib):
+    """The same at the 2-D radial shape of the inverse-NFFT workload (the
+    column kernels): 4096 of its nodes, N = 256^2, n = 512^2, m = 6."""
+    z = np.load(os.path.join(HERE, "golden", "cfg2_single_ref.npz"))
+    x, fh, f, idx = G.inputs_radial()
+    assert np.array_equal(idx, z["radial_idx"])
+    f_gpu, fhat_gpu = G.run(gpulib, True, G.N2, G.n2, G.m2, x, fh, f, idx)
+    q = Plan(gpulib, False, G.N2, len(x), n=G.n2, m=G.m2, flags=G.FLAGS)
+    q.x[:] = x.astype(np.float64)
+    q.f_hat[:] = fh.astype(np.complex128)
+    q.trafo_direct()
+    f_ndft = q.f.copy()
+    q.f[:] = f.astype(np.complex128)
+    q.adjoint_direct()
+    fhat_ndft = q.f_hat[idx].copy()
+    q.finalize()
+    e_ref_t, e_gpu_t = rel(z["radial_f_ref"], f_ndft), rel(f_gpu, f_ndft)
+    e_ref_a, e_gpu_a = rel(z["radial_fhat_ref"], fhat_ndft), rel(fhat_gpu, fhat_ndft)
+    print("radial 2-D trafo: reference nfftf %.2e, this library %.2e; adjoint: reference %.2e, this library %.2e"
           % (e_ref_t, e_gpu_t, e_ref_a, e_gpu_a))
     assert e_gpu_t <= 2 * e_ref_t, (e_gpu_t, e_ref_t)
     assert e_gpu_a <= 2 * e_ref_a, (e_gpu_a, e_ref_a)

@@ -78,7 +78,7 @@ enum {
   F_ALPHA_CGNE        // alpha = dot_r / dot_p (no reduction)
 };
 
-static constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+static constexpr int RED_BLOCKS = 152;  // one per SM: few partial sums for the finishing block
 static constexpr int RED_THREADS = 256;
 
 // ---------------------------------------------------------------- kernels

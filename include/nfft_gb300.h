@@ -174,8 +174,12 @@ void nfft_gb_kb_polyd_fit(int m, double b, int w, double *coef);
  * every GPU loading the library keeps until exit; the first call on a device
  * looks up its address there (make that call before any stream capture);
  * calls share the array, so calls that overlap on the GPU race and must be
- * serialised by the caller.  Returns 0 on success, -1 on invalid input, -2
- * if the scratch array cannot be reached on the current device. */
+ * serialised by the caller.  After cudaDeviceReset on a device the cached
+ * address is stale: do not call this there again in the same process.
+ * Returns 0 on success, -1 on invalid input, -2 if the scratch array cannot
+ * be reached on the current device or the CUDA context holds an error after
+ * the launches (reason in nfft_gb_last_error); a launch that fails inside
+ * goes through nfft_die and its hook, as every launch of this library. */
 int nfft_gb_sort_nodes_noalloc(int single, const void *x_dev, int d, const int *n, int m, int M,
                                long long *index_x_dev, void *stream);
 

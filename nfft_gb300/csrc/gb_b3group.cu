@@ -18,37 +18,23 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
   (void)poly;
   if constexpr (std::is_same<R, float>::value && W == 10) {
     if (adjoint) {
-      static bool attr_col = false;
-      if (!attr_col) {
-        GB_CUDA(cudaFuncSetAttribute(k_bt3_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_col = true;
-      }
+      set_smem_limit((const void *)k_bt3_col<W>, c3_smem_bytes<W>(g));
       k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly);
       GB_LAUNCHED("bt3_col");
       return;
     }
-    static bool attr_cell = false;
-    if (!attr_cell) {
-      GB_CUDA(cudaFuncSetAttribute(k_b3_cell<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr_cell = true;
-    }
+    set_smem_limit((const void *)k_b3_cell<W>, s3_smem_bytes<W>(g));
     k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.sst, perm, f, g, poly);
     GB_LAUNCHED("b3_cell");
     return;
   }
-  static bool attr = false;
   const size_t smem = adjoint ? g3_smem_bytes<R, W, G3_CS, true>(g) : g3_smem_bytes<R, W, G3_CS, false>(g);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_b3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024));
-    GB_CUDA(cudaFuncSetAttribute(k_bt3_group<R, W, G3_CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024));
-    attr = true;
-  }
   if (adjoint) {
+    set_smem_limit((const void *)k_bt3_group<R, W, G3_CS>, smem);
     k_bt3_group<R, W, G3_CS><<<nitems, G3_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
     GB_LAUNCHED("bt3_group");
   } else {
+    set_smem_limit((const void *)k_b3_group<R, W, G3_CS>, smem);
     k_b3_group<R, W, G3_CS><<<nitems, G3_THREADS, smem, s>>>(items, grid, xs, perm, f, g);
     GB_LAUNCHED("b3_group");
   }

@@ -154,8 +154,8 @@ static void batch_tables(Batch *b)
   GB_CUDA(cudaMalloc(&b->d_fhat_off, sizeof(long long) * np));
   GB_CUDA(cudaMemcpy(b->d_fhat_off, foff.data(), sizeof(long long) * np, cudaMemcpyHostToDevice));
   b->smem = smem;
-  GB_CUDA(cudaFuncSetAttribute(k_batch_b2, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  GB_CUDA(cudaFuncSetAttribute(k_batch_bt2, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  set_smem_limit((const void *)k_batch_b2, 96 * 1024);
+  set_smem_limit((const void *)k_batch_bt2, 96 * 1024);
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_bt2, BT_THREADS, smem));
   int dev = 0, sms = 0;
@@ -165,8 +165,8 @@ static void batch_tables(Batch *b)
   b->smem_col = smem_col;
   b->grid_ctas_col = 0;
   if (b->nitems_col) {
-    GB_CUDA(cudaFuncSetAttribute(k_batch_b2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
-    GB_CUDA(cudaFuncSetAttribute(k_batch_bt2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+    set_smem_limit((const void *)k_batch_b2c, smem_col);
+    set_smem_limit((const void *)k_batch_bt2c, smem_col);
     int per_sm_c = 0, per_sm_c2 = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, k_batch_bt2c, C2_THREADS, smem_col));
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c2, k_batch_b2c, C2_THREADS, smem_col));

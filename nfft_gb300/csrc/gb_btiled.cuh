@@ -228,13 +228,8 @@ template <typename R, int D, int W>
 static void run_b(const WorkItem *items, int nitems, const typename Cx<R>::T *grid, const R *xs,
                   const uint32_t *perm, typename Cx<R>::T *f, const Geom<R> &g, cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = tiled_smem_bytes_impl(g);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_b_tiled<R, D, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_b_tiled<R, D, W>, smem);
   k_b_tiled<R, D, W><<<nitems, 256, smem, s>>>(items, grid, xs, perm, f, g);
   GB_LAUNCHED("b_tiled");
 }
@@ -244,13 +239,8 @@ static void run_bt(const WorkItem *items, int nitems, typename Cx<R>::T *grid, c
                    const uint32_t *perm, const typename Cx<R>::T *f, const Geom<R> &g,
                    cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = tiled_smem_bytes_impl(g);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_bt_tiled<R, D, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_bt_tiled<R, D, W>, smem);
   k_bt_tiled<R, D, W><<<nitems, 256, smem, s>>>(items, grid, xs, perm, f, g);
   GB_LAUNCHED("bt_tiled");
 }

@@ -161,12 +161,8 @@ template <int W>
 static void run_bt2_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,
                       const double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = c2d_smem_bytes<W>();
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_bt2_col_d<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_bt2_col_d<W>, smem);
   k_bt2_col_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
   GB_LAUNCHED("bt2_col_d");
 }
@@ -227,12 +223,8 @@ template <int W>
 static void run_b2_d(const WorkItem *items, int nitems, const double2 *grid, const double *xs,
                      const uint32_t *perm, double2 *f, const Geom<double> &g, const WinPolyD &poly, cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = (size_t)C2<W>::EXT * C2<W>::SY * sizeof(double2);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_b2_node_d<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_b2_node_d<W>, smem);
   k_b2_node_d<W><<<nitems, C2D_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
   GB_LAUNCHED("b2_node_d");
 }
@@ -241,12 +233,8 @@ template <int W>
 static void run_bt2(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
                     const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = c2_smem_bytes<W>(true);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_bt2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_bt2_col<W>, smem);
   k_bt2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
   GB_LAUNCHED("bt2_col");
 }
@@ -255,12 +243,8 @@ template <int W>
 static void run_b2(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
                    float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
 {
-  static bool attr = false;
   const size_t smem = c2_smem_bytes<W>(false);
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_b2_col<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_b2_col<W>, smem);
   k_b2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
   GB_LAUNCHED("b2_col");
 }

@@ -25,6 +25,11 @@ template <> struct Cx<double> { typedef double2 T; };
 // ---------------------------------------------------------------- errors
 void record_error(const char *fmt, ...);
 void fatal(const char *fmt, ...);  // records, then calls nfft_die (exits)
+// Raises `kernel`'s dynamic shared-memory limit to at least `bytes` on the
+// current device.  The attribute is per device, so this keeps one record per
+// (device, kernel) and sets it where it is still lower; a mutex makes first
+// calls from several host threads safe.
+void set_smem_limit(const void *kernel, size_t bytes);
 void check_cuda(cudaError_t e, const char *what, const char *file, int line);
 void check_launch(const char *what, const char *file, int line);
 

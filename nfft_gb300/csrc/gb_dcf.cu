@@ -300,11 +300,7 @@ int nfft_gb_mlp_grad(const float *params, const float *feat, const float *target
   GB_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), s));
   if (M <= 0) return M < 0 ? -1 : 0;
   const size_t smem = mlp_grad_smem_floats() * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    GB_CUDA(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_smem_limit((const void *)k_mlp_grad, smem);
   const int blocks = std::min((M + MLP_THREADS - 1) / MLP_THREADS, 152);
   k_mlp_grad<<<blocks, MLP_THREADS, smem, s>>>(params, feat, target, M, grad, loss);
   GB_LAUNCHED("mlp_grad");

@@ -18,10 +18,16 @@
 //  * the first call on a device looks up the array's device address there
 //    (cudaGetSymbolAddress, with that device current) and caches it; make that
 //    first call before any stream capture;
+//  * the cached address belongs to the device's current context: after
+//    cudaDeviceReset on a device, do not call this entry point there again
+//    in the same process;
 //  * all calls share the array, which keeps the last call's contents; calls
 //    that overlap on the GPU (other streams, other threads) race on it, so
 //    serialise them.  Nothing in the array has to start at zero: every
-//    intermediate is fully written before it is read.
+//    intermediate is fully written before it is read;
+//  * a kernel launch that fails inside goes through nfft_die (and its die
+//    hook) like every launch of this library; an error left in the CUDA
+//    context after the launches is returned as -2.
 #include <cstring>
 #include <mutex>
 
@@ -43,7 +49,15 @@ void *g_noalloc_ptr[64];  // device address of the scratch array, per device
 void *scratch_for_current_device()
 {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  const cudaError_t ge = cudaGetDevice(&dev);
+  if (ge != cudaSuccess) {
+    gb::record_error("nfft_gb_sort_nodes_noalloc: cudaGetDevice failed: %s", cudaGetErrorString(ge));
+    return nullptr;
+  }
+  if (dev < 0 || dev >= 64) {
+    gb::record_error("nfft_gb_sort_nodes_noalloc: device %d is beyond the 64 devices it serves", dev);
+    return nullptr;
+  }
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void *p = nullptr;
@@ -71,6 +85,12 @@ int sort_noalloc(const R *x_dev, int d, const int *n, int m, int M, long long *i
   g.n_total = 1;
   for (int t = 0; t < GB_MAXD; ++t) {
     const int nt = t < d ? n[t] : 1;
+    // keys are 32-bit: the product of the n_t must stay below 2^32 (checked
+    // before each multiplication, so it cannot overflow)
+    if (t < d && g.n_total > 0xffffffffLL / nt) {
+      gb::record_error("nfft_gb_sort_nodes_noalloc: n_0 * ... * n_{d-1} must be below 2^32");
+      return -1;
+    }
     g.n[t] = nt;
     g.N[t] = nt;
     g.nR[t] = (R)nt;
@@ -82,10 +102,6 @@ int sort_noalloc(const R *x_dev, int d, const int *n, int m, int M, long long *i
   g.cs = 1;
   g.csz = 1;
   g.sub = 1;
-  if (g.n_total > 0xffffffffLL) {
-    gb::record_error("nfft_gb_sort_nodes_noalloc: n_0 * ... * n_{d-1} must be below 2^32");
-    return -1;
-  }
   unsigned char *base = (unsigned char *)scratch_for_current_device();
   if (!base) return -2;
   if (M == 0) return 0;
@@ -106,6 +122,12 @@ int sort_noalloc(const R *x_dev, int d, const int *n, int m, int M, long long *i
   while ((1LL << bits) < g.n_total) ++bits;
   gb::radix_sort_pairs(k1, v1, k2, v2, Mz, bits > 0 ? bits : 1, temp, s);
   gb::launch_ref_index_to_int64(k1, v1, M, index_x_dev, s);
+  const cudaError_t le = cudaPeekAtLastError();
+  if (le != cudaSuccess) {
+    gb::record_error("nfft_gb_sort_nodes_noalloc: CUDA error after the sort's launches: %s",
+                     cudaGetErrorString(le));
+    return -2;
+  }
   return 0;
 }
 

@@ -19,8 +19,10 @@
 #include <cstring>
 #include <ctime>
 #include <mutex>
+#include <map>
 #include <string>
 #include <unordered_set>
+#include <utility>
 
 #include "../../include/nfft3.h"
 #include "gb_common.cuh"
@@ -105,6 +107,20 @@ void check_launch(const char *what, const char *file, int line)
 {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) fatal("launch of %s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+void set_smem_limit(const void *kernel, size_t bytes)
+{
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice", __FILE__, __LINE__);
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &have = done[std::make_pair(dev, kernel)];
+  if (have >= bytes) return;
+  check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+             "cudaFuncSetAttribute", __FILE__, __LINE__);
+  have = bytes;
 }
 
 }  // namespace gb

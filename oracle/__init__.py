@@ -18,7 +18,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = os.environ.get("NFFT_REFERENCE_SRC", "/root/reference")
+# The reference checkout: NFFT_REFERENCE_SRC, else a "reference" directory
+# beside this repository's root.
+REFERENCE_SRC = os.environ.get("NFFT_REFERENCE_SRC") or os.path.normpath(
+    os.path.join(HERE, os.pardir, os.pardir, "reference"))
 
 ORC_SORT = 1
 ORC_BLOCKWISE = 2

@@ -11,10 +11,12 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+import oracle  # noqa: E402  (the reference checkout's location)
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NFFT_REFERENCE_SRC", "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else oracle.REFERENCE_SRC
     with open(os.path.join(root, "tests", "bessel.c")) as fh:
         text = fh.read()
     body = text[text.index("static const R r[]"):]

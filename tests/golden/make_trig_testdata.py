@@ -14,6 +14,8 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+import oracle  # noqa: E402  (the reference checkout's location)
 
 
 def parse(text, sine):
@@ -30,7 +32,7 @@ def parse(text, sine):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NFFT_REFERENCE_SRC", "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else oracle.REFERENCE_SRC
     out = {}
     files = sorted(glob.glob(os.path.join(root, "tests", "data", "nfct_*.txt"))
                    + glob.glob(os.path.join(root, "tests", "data", "nfst_*.txt")))

@@ -40,11 +40,13 @@ def _regular_index(lib, single, N, x, m):
 
 @pytest.mark.parametrize("single", [True, False])
 def test_noalloc_sort_matches_precompute_twice(gpulib, single):
-    torch = pytest.importorskip("torch")
+    import torch  # a GPU run without torch fails here rather than skipping
     fn = _entry(gpulib)
     dev = torch.device("cuda", 0)
     dt = torch.float32 if single else torch.float64
-    cases = [([32, 32, 32], 200000, 4, 7), ([64, 48], 150000, 6, 8)]  # two calls in a row
+    # calls in a row on the shared scratch array; the last at the stated
+    # maximum of 2^18 nodes, where its room is tightest
+    cases = [([32, 32, 32], 200000, 4, 7), ([64, 48], 150000, 6, 8), ([64, 64, 64], 1 << 18, 4, 9)]
     for N, M, m, seed in cases:
         rng = np.random.default_rng(seed)
         x = rng.uniform(-0.5, 0.5, size=(M, len(N)))
@@ -68,3 +70,14 @@ def test_noalloc_sort_rejects_too_many_nodes(gpulib):
     assert rc == -1
     gpulib.nfft_gb_last_error.restype = C.c_char_p
     assert b"exceeds the maximum" in gpulib.nfft_gb_last_error()
+
+
+def test_noalloc_sort_rejects_grid_beyond_32bit_keys(gpulib):
+    fn = _entry(gpulib)
+    # 65536 * 65536 * 2 = 2^33 grid points: the 32-bit sort keys cannot hold
+    # them; rejected on the host before any multiplication can overflow
+    n = (C.c_int * 3)(65536, 65536, 2)
+    rc = fn(1, None, 3, n, 4, 0, None, None)
+    assert rc == -1
+    gpulib.nfft_gb_last_error.restype = C.c_char_p
+    assert b"below 2^32" in gpulib.nfft_gb_last_error()

@@ -13,7 +13,7 @@ all M nodes; value = nodes per step / step time (whole job over all ranks).
           arrays, host<->device copies inside the timed region;
 * cpu_baseline / --impl reference: the oracle's OpenMP restatement of the
           reference algorithm (PRE_PSI tables, sorted nodes, blockwise
-          adjoint) on this host's cores, on a bounded node sample.
+          adjoint) on all of this host's cores, over the whole workload.
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -34,29 +34,30 @@ sys.path.insert(0, ROOT)
 
 METRIC = "nodes/s fwd+adj, %HBM roofline; iNFFT time to 1e-5 rel. err: learned vs plain"
 UNIT = "nodes/s"
-CPU_SAMPLE_M = 1 << 20
 
 
 def workload(name):
+    k3 = ("k_b3_cell", "k_bt3_col")
     if name == "small":  # for profiler captures of the same kernels
         return dict(name="3-D NFFT FP32 N=64^3 n=128^3 m=4 M=2^21 uniform", d=3, N=[64] * 3,
-                    n=[128] * 3, m=4, M=1 << 21, dist="uniform")
+                    n=[128] * 3, m=4, M=1 << 21, dist="uniform", kernels=k3, l2="inputs larger than L2 "
+                    "(x 25 MB, grid 16.8 MB, f 16.8 MB: not all); profiler captures only")
+    if name == "radial-pair":  # the inverse-NFFT workload's transforms (2-D column kernels)
+        return dict(name="2-D NFFT FP32 N=256^2 n=512^2 m=6 radial 402x512", d=2, N=[256, 256], n=[512, 512],
+                    m=6, M=402 * 512, dist="radial", kernels=("k_b2_col", "k_bt2_col"),
+                    l2="L2-resident: grid 2.1 MB, nodes 1.6 MB, f 1.6 MB stay in L2 between steps, as "
+                       "they do between the steps of the iterative inverse NFFT")
     dist = "clustered" if name == "clustered" else "uniform"
     return dict(name="3-D NFFT FP32 N=128^3 n=256^3 m=4 M=2^24 %s" % dist, d=3, N=[128] * 3,
-                n=[256] * 3, m=4, M=1 << 24, dist=dist)
+                n=[256] * 3, m=4, M=1 << 24, dist=dist, kernels=k3,
+                l2="inputs larger than L2 (x 201 MB, grid 134 MB, f 134 MB per rank); no flush")
 
 
 def make_nodes(wl, seed):
-    rng = np.random.default_rng(seed)
-    M, d = wl["M"], wl["d"]
-    if wl["dist"] == "uniform":
-        x = rng.uniform(-0.5, 0.5, size=(M, d)).astype(np.float32)
-    else:  # mixture of 32 isotropic Gaussians, std 0.02, wrapped to the torus
-        c = rng.uniform(-0.5, 0.5, size=(32, d))
-        x = c[rng.integers(0, 32, M)] + 0.02 * rng.standard_normal((M, d))
-        x = (((x + 0.5) % 1.0) - 0.5).astype(np.float32)
-        x[x >= 0.5] = -0.5
-    return x
+    from nfft_gb300 import workloads
+    if wl["dist"] == "radial":
+        return workloads.radial_nodes(402, 512).astype(np.float32)
+    return workloads.cube_nodes(wl["M"], wl["d"], wl["dist"], seed)
 
 
 def algorithmic_bytes_B(wl):
@@ -136,24 +137,25 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_pair(wl, x, sample_m, steps, warmup):
-    """Time the oracle's restatement of the reference (OpenMP, PRE_PSI,
-    sorted nodes, blockwise adjoint) on `sample_m` nodes of the workload with
-    the full grid; extrapolate B / B^T linearly in M, keep D and FFT as
-    measured (they do not depend on M).  Returns per-step dicts."""
+def cpu_pair(wl, x, steps, warmup):
+    """Time the oracle's restatement of the reference (OpenMP over all host
+    cores, PRE_PSI tables, sorted nodes, the blockwise adjoint) on the whole
+    workload: node set-up once, then warmup + steps trafo + adjoint pairs, as
+    the reference's examples/nfft/nfft_benchomp_detail.c:96-118 times them
+    (D, FFT and B of each call from its stage timers).  Returns per-step dicts
+    and the set-up time."""
     import oracle
-    o = oracle.OraclePlan(wl["N"], sample_m, n=wl["n"], m=wl["m"], single=True, sort=True,
+    o = oracle.OraclePlan(wl["N"], wl["M"], n=wl["n"], m=wl["m"], single=True, sort=True,
                           blockwise=True, pre_psi=True)
-    o.set_nodes(x[:sample_m])
+    o.set_nodes(x)
     t0 = time.perf_counter()
     o.precompute()
     t_pre = time.perf_counter() - t0
     rng = np.random.default_rng(1)
     NN = int(np.prod(wl["N"]))
     fh = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
-    f = (rng.uniform(-1, 1, sample_m) + 1j * rng.uniform(-1, 1, sample_m)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, wl["M"]) + 1j * rng.uniform(-1, 1, wl["M"])).astype(np.complex64)
     out = []
-    scale = wl["M"] / sample_m
     for it in range(warmup + steps):
         t0 = time.perf_counter()
         o.trafo(fh)
@@ -162,14 +164,23 @@ def cpu_pair(wl, x, sample_m, steps, warmup):
         o.adjoint(f)
         t2 = time.perf_counter()
         st_a = o.stage_times()
-        fixed = st_t[0] + st_t[1] + st_a[0] + st_a[1]
-        b = st_t[2] + st_a[2]
-        full = fixed + b * scale
         if it >= warmup:
-            out.append(dict(pair_s=t2 - t0, fixed_s=fixed, b_s=b, full_s=full,
-                            nodes_per_s=wl["M"] / full))
+            out.append(dict(pair_s=t2 - t0, trafo_s=t1 - t0, adjoint_s=t2 - t1,
+                            stages_s={"trafo_D": st_t[0], "trafo_FFT": st_t[1], "trafo_B": st_t[2],
+                                      "adjoint_BT": st_a[2], "adjoint_FFT": st_a[1], "adjoint_DT": st_a[0]},
+                            nodes_per_s=wl["M"] / (t2 - t0)))
     o.close()
     return out, t_pre
+
+
+def cpu_summary(wl, steps, t_pre):
+    """Median pair rate and stage times of cpu_pair's steps."""
+    rate = statistics.median(s["nodes_per_s"] for s in steps)
+    stages = {k: round(1e3 * statistics.median(s["stages_s"][k] for s in steps), 2) for k in steps[0]["stages_s"]}
+    sample = ("oracle OpenMP restatement of the reference (PRE_PSI tables, sorted nodes, blockwise adjoint, "
+              "project radix-2 FFT) on all %d nodes with the full grid, %d threads; median of %d "
+              "trafo + adjoint pairs after the node set-up (%.1f s)" % (wl["M"], cpu_cores(), len(steps), t_pre))
+    return rate, stages, sample
 
 
 def cpu_cores():
@@ -184,23 +195,17 @@ def run_reference(args, wl):
     if rank != 0:
         return 0
     x = make_nodes(wl, 0)
-    steps, t_pre = cpu_pair(wl, x, min(CPU_SAMPLE_M, wl["M"]), args.steps, args.warmup)
-    vals = [s["nodes_per_s"] for s in steps]
-    value = statistics.median(vals)
-    ms = statistics.mean(s["full_s"] for s in steps) * 1e3
-    cores = cpu_cores()
-    sample = ("oracle OpenMP restatement of the reference (PRE_PSI, sorted nodes, blockwise adjoint, "
-              "project radix-2 FFT) on the first %d of %d nodes with the full 256^3 grid; B and B^T "
-              "time scaled by M/%d, D and FFT as measured; %d threads"
-              % (CPU_SAMPLE_M, wl["M"], CPU_SAMPLE_M, cores))
+    steps, t_pre = cpu_pair(wl, x, args.steps, args.warmup)
+    value, stages, sample = cpu_summary(wl, steps, t_pre)
+    ms = statistics.mean(s["pair_s"] for s in steps) * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config_of(wl),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "precompute_s_sample": t_pre}
+            "stages_ms_median": stages, "precompute_s": round(t_pre, 3)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -208,8 +213,7 @@ def run_reference(args, wl):
 def config_of(wl):
     return {"workload": wl["name"], "d": wl["d"], "N": wl["N"], "n": wl["n"], "m": wl["m"],
             "M": wl["M"], "nodes": wl["dist"], "precision": "complex64",
-            "window": "Kaiser-Bessel", "l2_between_steps": "inputs larger than L2 (x 201 MB, "
-            "grid 134 MB, f 134 MB per rank); no flush"}
+            "window": "Kaiser-Bessel", "l2_between_steps": wl["l2"]}
 
 
 # ------------------------------------------------------------------ GPU side
@@ -347,7 +351,7 @@ def run_gpu(args, wl):
     sums = (C.c_float * 7)()
     counts = (C.c_int * 2)()
     end(pa, sums, counts)
-    # trafo: k_d_pad + k_b3_cell; adjoint: k_bt3_col + k_d_crop (cuFFT and memsets not counted)
+    # trafo: k_d_pad + B; adjoint: B^T + k_d_crop (cuFFT and memsets not counted)
     launches = 4 * args.steps
     ms_step, value = replica_rate(ms_total, M, args.steps, dist, dev)
 
@@ -378,7 +382,7 @@ def run_gpu(args, wl):
              "adjoint_memset_ms": sums[3] / nA, "adjoint_BT_ms": sums[4] / nA,
              "adjoint_FFT_ms": sums[5] / nA, "adjoint_DT_ms": sums[6] / nA}
     b_ms, bt_ms = stage["trafo_B_ms"], stage["adjoint_BT_ms"]
-    kb, kbt = ("k_b3_cell", "k_bt3_col") if wl["d"] == 3 else ("k_b_tiled", "k_bt_tiled")
+    kb, kbt = wl["kernels"]
     dom, dom_ms = (kbt + " (B^T spreading)", bt_ms) if bt_ms >= b_ms else (kb + " (B interpolation)", b_ms)
     peaks, peak_kind = measured_peaks()
     bytes_b = algorithmic_bytes_B(wl)
@@ -406,11 +410,10 @@ def run_gpu(args, wl):
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        steps, _ = cpu_pair(wl, x, min(CPU_SAMPLE_M, M), 2, 1)
-        v = statistics.median(s["nodes_per_s"] for s in steps)
-        cpu = {"value": v, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
-               "sample": "oracle OpenMP restatement of the reference on the first %d nodes with the "
-                         "full grid; B/B^T scaled by M/%d, D and FFT as measured" % (CPU_SAMPLE_M, CPU_SAMPLE_M)}
+        steps, t_pre_cpu = cpu_pair(wl, x, 5, 1)
+        v, stages_cpu, sample = cpu_summary(wl, steps, t_pre_cpu)
+        cpu = {"value": v, "unit": UNIT, "cores": cpu_cores(), "kind": "port", "sample": sample,
+               "stages_ms_median": stages_cpu}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -655,7 +658,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
-                    choices=["uniform", "clustered", "small", "infft", "learned", "batched"])
+                    choices=["uniform", "clustered", "small", "radial-pair", "infft", "learned", "batched"])
     ap.add_argument("--plans", type=int, default=1024, help="plans of the batched workload")
     ap.add_argument("--train", type=int, default=256, help="training trajectories (learned)")
     ap.add_argument("--test", type=int, default=8, help="held-out trajectories (learned)")

@@ -23,6 +23,14 @@ extern "C" {
 /* Run the plan on this cudaStream_t (NULL = the plan's own stream). */ \
 int X(gb_set_stream)(X(plan) *ths, void *cuda_stream); \
 void *X(gb_get_stream)(X(plan) *ths); \
+/* Compensated adjoint of single-precision 2-D plans on the column kernels \
+ * (no counterpart in the reference, whose double build needs none): the \
+ * shared-memory subgrid keeps a second plane of rounding errors (error-free \
+ * sums), the write-back adds them into the grid by error-free compare-and-swap \
+ * with the remaining errors folded in before the FFT.  mode 1 on, 0 off, -1 \
+ * the default (on for cut-off m >= 6).  Returns 0, or -1 (nothing changed) \
+ * for a plan without such a kernel (double precision, d != 2, NDFT). */ \
+int X(gb_set_compensated)(X(plan) *ths, int mode); \
 /* Device buffers of the plan: f_hat (N_total complex), f (M_total complex), \
  * in the caller's natural orders, and x (M_total*d reals, node-major). */ \
 void *X(gb_device_f_hat)(X(plan) *ths); \
@@ -159,6 +167,14 @@ void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef);
  * + k] (k < 17), the degree-16 interpolant at the 17 Chebyshev points,
  * computed in extended precision and rounded to double.  Host only. */
 void nfft_gb_kb_polyd_fit(int m, double b, int w, double *coef);
+
+/* Bounded waits of the 3-D single-precision transforms that gave up since
+ * the last call (no counterpart in the reference).  Their B kernel stages
+ * each tile of the oversampled grid with a TMA copy and waits for it at most
+ * about a second; a copy that never arrives leaves that tile's samples
+ * unwritten and is counted here instead of hanging the GPU.  Reads and
+ * clears the count of the current device; 0 in every correct run. */
+unsigned long long nfft_gb_tma_wait_timeouts(void);
 
 /* The node sort of NFFT_SORT_NODES without any device allocation (no
  * counterpart in the reference).  For callers that cannot allocate device

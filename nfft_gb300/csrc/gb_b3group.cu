@@ -1,12 +1,26 @@
 // gb_b3group.cu -- instantiations and launchers of the 3-D sub-cell group
 // kernels (see gb_b3group.cuh).
 #include <algorithm>
+#include <cstring>
 #include <type_traits>
 
 #include "gb_b3group.cuh"
 #include "gb_col3.cuh"
 
 namespace gb {
+
+int col3_b_ext_y(int w)
+{
+  return w == 10 ? S3<10>::EXTY : 8 + w - 1;
+}
+
+unsigned long long read_wait_timeouts()
+{
+  unsigned long long v = 0, z = 0;
+  GB_CUDA(cudaMemcpyFromSymbol(&v, g_tma_wait_timeouts, sizeof(v)));
+  GB_CUDA(cudaMemcpyToSymbol(g_tma_wait_timeouts, &z, sizeof(z)));
+  return v;
+}
 
 static constexpr int G3_CS = 2;  // sub-cell edge
 
@@ -17,14 +31,21 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
 {
   (void)poly;
   if constexpr (std::is_same<R, float>::value && W == 10) {
+    // the grid's TMA view (a zeroed map and use_tma = 0 where there is none)
+    CUtensorMap gmap;
+    memset(&gmap, 0, sizeof(gmap));
+    const int use_tma = cb.grid_map && cb.grid_map_b ? 1 : 0;
+    if (use_tma) gmap = adjoint ? *cb.grid_map : *cb.grid_map_b;
     if (adjoint) {
       set_smem_limit((const void *)k_bt3_col<W>, c3_smem_bytes<W>(g));
-      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly);
+      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly,
+                                                                   gmap, use_tma);
       GB_LAUNCHED("bt3_col");
       return;
     }
     set_smem_limit((const void *)k_b3_cell<W>, s3_smem_bytes<W>(g));
-    k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.sst, perm, f, g, poly);
+    k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.sst, perm, f, g, poly,
+                                                                 gmap, use_tma);
     GB_LAUNCHED("b3_cell");
     return;
   }

@@ -2,21 +2,32 @@
 // and B (interpolation) by x-row strips of sub-cell columns: the per-plan
 // kernels.  The single-precision work-item functions and their design are in
 // gb_col2.cuh.
+#include <algorithm>
+
 #include "gb_col2.cuh"
 
 namespace gb {
 
 // per-plan kernels: one CTA per work item
-template <int W>
+template <int W, bool COMP>
 __global__ void __launch_bounds__(C2_THREADS, 3) k_bt2_col(const WorkItem *__restrict__ items,
                                                             float2 *__restrict__ grid,
                                                             const float *__restrict__ xs,
                                                             const uint32_t *__restrict__ perm,
                                                             const float2 *__restrict__ f, Geom<float> g,
-                                                            WinPoly poly)
+                                                            WinPoly poly, float2 *__restrict__ grid_lo)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  c2_bt_item<W>(items[blockIdx.x], grid, xs, perm, f, g, poly, smem_raw);
+  c2_bt_item<W, COMP>(items[blockIdx.x], grid, xs, perm, f, g, poly, smem_raw, grid_lo);
+}
+
+// grid += grid_lo: the compensated B^T's rounding errors folded in before the FFT
+__global__ void k_fold_lo(float2 *__restrict__ grid, const float2 *__restrict__ lo, long long n)
+{
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const float2 a = grid[k], b = lo[k];
+    grid[k] = make_float2(a.x + b.x, a.y + b.y);
+  }
 }
 
 template <int W>
@@ -231,11 +242,21 @@ static void run_b2_d(const WorkItem *items, int nitems, const double2 *grid, con
 
 template <int W>
 static void run_bt2(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
-                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s, float2 *grid_lo)
 {
+  if (grid_lo) {
+    const size_t smem = c2_smem_bytes<W>(true, true);
+    set_smem_limit((const void *)k_bt2_col<W, true>, smem);
+    k_bt2_col<W, true><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly, grid_lo);
+    GB_LAUNCHED("bt2_col (compensated)");
+    const long long n = (long long)g.n[0] * g.n[1];
+    k_fold_lo<<<(unsigned)std::min<long long>((n + 255) / 256, 1216), 256, 0, s>>>(grid, grid_lo, n);
+    GB_LAUNCHED("fold_lo");
+    return;
+  }
   const size_t smem = c2_smem_bytes<W>(true);
-  set_smem_limit((const void *)k_bt2_col<W>, smem);
-  k_bt2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
+  set_smem_limit((const void *)k_bt2_col<W, false>, smem);
+  k_bt2_col<W, false><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly, nullptr);
   GB_LAUNCHED("bt2_col");
 }
 
@@ -265,13 +286,13 @@ int col2_column_width(int w)
 }
 
 void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
-                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s, float2 *grid_lo)
 {
   if (nitems <= 0) return;
   switch (g.w) {
-#define GB_C2_RUN(W)                                                 \
-  case W:                                                            \
-    run_bt2<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
+#define GB_C2_RUN(W)                                                          \
+  case W:                                                                     \
+    run_bt2<W>(items, nitems, grid, xs, perm, f, g, poly, s, grid_lo); \
     return;
     GB_COL2_WIDTHS(GB_C2_RUN)
 #undef GB_C2_RUN

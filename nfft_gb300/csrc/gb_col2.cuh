@@ -66,12 +66,42 @@ struct C2 {
   static_assert(W % 2 == 0 && W <= KB_POLY_WMAX, "even window with a polynomial form");
 };
 
+// comp: B^T with a compensated subgrid (a second plane of rounding errors)
 template <int W>
-inline size_t c2_smem_bytes(bool adjoint)
+inline size_t c2_smem_bytes(bool adjoint, bool comp = false)
 {
   typedef C2<W> P;
   return (size_t)C2_WARPS * (adjoint ? P::WARP_FLOATS_T : P::WARP_FLOATS_B) * sizeof(float)
-         + (size_t)P::EXT * P::SY * sizeof(float2);
+         + (size_t)(comp ? 2 : 1) * P::EXT * P::SY * sizeof(float2);
+}
+
+// s = a + b rounded, and its rounding error e (a + b = s + e exactly): the
+// error-free sum (TwoSum, Knuth), componentwise, in separately rounded steps
+__device__ __forceinline__ float2 c2_two_sum(float2 a, float2 b, float2 &s)
+{
+  s = make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+  const float bx = __fsub_rn(s.x, a.x), by = __fsub_rn(s.y, a.y);
+  return make_float2(__fadd_rn(__fsub_rn(a.x, __fsub_rn(s.x, bx)), __fsub_rn(b.x, bx)),
+                     __fadd_rn(__fsub_rn(a.y, __fsub_rn(s.y, by)), __fsub_rn(b.y, by)));
+}
+
+// *p += v by 64-bit compare-and-swap on the complex cell; returns the
+// rounding error of the add that went in
+__device__ __forceinline__ float2 c2_cas_add_err(float2 *p, float2 v)
+{
+  unsigned long long *u = reinterpret_cast<unsigned long long *>(p);
+  unsigned long long old = *reinterpret_cast<volatile unsigned long long *>(u);
+  for (;;) {
+    union {
+      unsigned long long u;
+      float2 f;
+    } cur, nxt;
+    cur.u = old;
+    const float2 e = c2_two_sum(cur.f, v, nxt.f);
+    const unsigned long long seen = atomicCAS(u, cur.u, nxt.u);
+    if (seen == old) return e;
+    old = seen;
+  }
 }
 
 __device__ __forceinline__ unsigned long long c2_bits(float2 v)
@@ -89,8 +119,13 @@ __device__ __forceinline__ unsigned long long c2_bits(float2 v)
 // four is read, summed and offered by one 64-bit compare-and-swap before any
 // result is checked; a cell another warp changed in between is added again
 // with the atomic add of each component.  Zero cells are skipped.
-template <int HP>
-__device__ __forceinline__ void c2_flush(float2 *p, const float2 (&vr)[HP], const float2 (&vi)[HP], int nv)
+// COMP: the compensated form for wide windows -- every add into p is
+// error-free transformed and its rounding error is added into plo, the
+// subgrid's error plane, so p + plo carries the column sums to about twice
+// single precision.
+template <int HP, bool COMP = false>
+__device__ __forceinline__ void c2_flush(float2 *p, const float2 (&vr)[HP], const float2 (&vi)[HP], int nv,
+                                         float2 *plo = nullptr)
 {
   constexpr int N = 2 * HP, ZB = 4;
   volatile float2 *vp = p;
@@ -112,14 +147,25 @@ __device__ __forceinline__ void c2_flush(float2 *p, const float2 (&vr)[HP], cons
       }
     }
     unsigned miss = 0;
+    float2 err[ZB];
 #pragma unroll
     for (int q = 0; q < ZB; ++q)
       if (on[q]) {
+        float2 sum;
+        if (COMP) err[q] = c2_two_sum(cur[q], v[q], sum);
+        else sum = __fadd2_rn(cur[q], v[q]);
         const unsigned long long old = c2_bits(cur[q]);
-        const unsigned long long want = c2_bits(__fadd2_rn(cur[q], v[q]));
-        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + e0 + q), old, want) != old) miss |= 1u << q;
+        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + e0 + q), old, c2_bits(sum)) != old) miss |= 1u << q;
       }
-    if (miss) {
+    if (COMP) {
+#pragma unroll
+      for (int q = 0; q < ZB; ++q)
+        if (on[q]) {
+          // a cell another warp changed in between: add again, with its error
+          if ((miss >> q) & 1u) err[q] = c2_cas_add_err(p + e0 + q, v[q]);
+          if (err[q].x != 0.f || err[q].y != 0.f) c2_cas_add_err(plo + e0 + q, err[q]);
+        }
+    } else if (miss) {
 #pragma unroll
       for (int q = 0; q < ZB; ++q)
         if ((miss >> q) & 1u) {
@@ -128,6 +174,17 @@ __device__ __forceinline__ void c2_flush(float2 *p, const float2 (&vr)[HP], cons
         }
     }
   }
+}
+
+// The compensated write-back of one subgrid cell (hi, lo): hi goes into the
+// grid by compare-and-swap with its rounding error, which joins lo in the
+// grid's error plane (plain atomic adds: the error plane's own rounding is
+// below single precision of the errors)
+__device__ __forceinline__ void c2_global_add_comp(float2 *g, float2 *glo, float2 hi, float2 lo)
+{
+  const float2 e = c2_cas_add_err(g, hi);
+  const float2 t = make_float2(__fadd_rn(e.x, lo.x), __fadd_rn(e.y, lo.y));
+  if (t.x != 0.f || t.y != 0.f) global_add_c(glo, t);
 }
 
 // Set-up of one node (lane j of a task): its column in the tile at
@@ -161,13 +218,16 @@ __device__ __forceinline__ int c2_setup(const float *x, const Geom<float> &g, in
   return (ux / P::CX) * C2_SLABS + uy / C2_CY;
 }
 
-// B^T of one work item by a CTA of C2_THREADS threads with c2_smem_bytes<W>(true)
-// bytes of shared memory at smem_raw; adds the item's subgrid to grid.
-template <int W>
+// B^T of one work item by a CTA of C2_THREADS threads with
+// c2_smem_bytes<W>(true, COMP) bytes of shared memory at smem_raw; adds the
+// item's subgrid to grid.  COMP: the compensated form (subgrid error plane,
+// error-free adds into grid with the errors into grid_lo, which the caller
+// folds into grid afterwards).
+template <int W, bool COMP = false>
 __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restrict__ grid,
                                            const float *__restrict__ xs, const uint32_t *__restrict__ perm,
                                            const float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
-                                           unsigned char *smem_raw)
+                                           unsigned char *smem_raw, float2 *__restrict__ grid_lo = nullptr)
 {
   typedef C2<W> P;
   constexpr int CX = P::CX, HP = P::HP, SY = P::SY;
@@ -176,9 +236,10 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
   float *const wx = base + warp * P::WARP_FLOATS_T;  // real, stride XS
   float *const wy = wx + P::XS * C2_CHUNK;
   float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_T);
+  float2 *const sgl = sg + P::EXT * SY;  // error plane (COMP only)
 
   const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
-  for (int i = threadIdx.x; i < P::EXT * SY; i += C2_THREADS) sg[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < (COMP ? 2 : 1) * P::EXT * SY; i += C2_THREADS) sg[i] = make_float2(0.f, 0.f);
   __syncthreads();
   const int h = lane >> 4, r = lane & 15;
 
@@ -219,7 +280,8 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
         }
       }
       const int xc = c / C2_SLABS, sl = c - xc * C2_SLABS;
-      if (r < P::ROWS) c2_flush<HP>(sg + (CX * xc + r) * SY + C2_CY * sl + 2 * h * HP, ar, ai, P::NPOS - 2 * h * HP);
+      const int off = (CX * xc + r) * SY + C2_CY * sl + 2 * h * HP;
+      if (r < P::ROWS) c2_flush<HP, COMP>(sg + off, ar, ai, P::NPOS - 2 * h * HP, sgl + off);
     }
     __syncwarp();  // the next task's set-up reuses the vectors
   }
@@ -227,11 +289,14 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
   for (int idx = threadIdx.x; idx < P::EXT * P::EXT; idx += C2_THREADS) {
     const int rx = idx / P::EXT, ry = idx - rx * P::EXT;
     const float2 v = sg[rx * SY + ry];
-    if (v.x != 0.f || v.y != 0.f) {
+    const float2 vl = COMP ? sgl[rx * SY + ry] : make_float2(0.f, 0.f);
+    if (v.x != 0.f || v.y != 0.f || vl.x != 0.f || vl.y != 0.f) {
       int p0 = org0 + rx, p1 = org1 + ry;
       while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
       while (p1 >= g.n[1]) p1 -= g.n[1];
-      global_add_c(grid + (long long)p0 * g.n[1] + p1, v);
+      const long long q = (long long)p0 * g.n[1] + p1;
+      if (COMP) c2_global_add_comp(grid + q, grid_lo + q, v, vl);
+      else global_add_c(grid + q, v);
     }
   }
 }

@@ -33,14 +33,22 @@
 //    time; here a row's complex cells are read, summed and swapped as 64-bit
 //    words, all of them before the first result is checked, and only the
 //    rare cell another warp changed in between is added again;
-//  * the subgrid goes to the global grid once per work item with vector
-//    reductions.
+//  * the subgrid goes to the global grid once per work item: a tile whose
+//    padded box lies inside the grid is copied into a dense box in the
+//    warps' (then idle) scratch and added to the grid by one TMA add-reduce
+//    (cp.reduce.async.bulk.tensor); a tile whose box wraps around the grid
+//    edge adds its cells with vector reductions.
 #pragma once
 
 #include "gb_b3group.cuh"  // warp_transpose_reduce
 #include "gb_internal.h"
+#include "gb_tma.cuh"
 
 namespace gb {
+
+// bounded TMA waits that gave up (read and cleared by read_wait_timeouts);
+// this header is compiled into one unit (gb_b3group.cu)
+__device__ unsigned long long g_tma_wait_timeouts;
 
 static constexpr int C3_THREADS = 256;
 static constexpr int C3_WARPS = C3_THREADS / 32;
@@ -150,12 +158,13 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
                                                             const uint16_t *__restrict__ cst,
                                                             const uint32_t *__restrict__ perm,
                                                             const float2 *__restrict__ f, Geom<float> g,
-                                                            WinPoly poly)
+                                                            WinPoly poly, const __grid_constant__ CUtensorMap gmap,
+                                                            int use_tma)
 {
   typedef C3<W> P;
   constexpr int EXT = P::EXT, BOXP = P::BOXP, RPL = P::RPL;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *const base = reinterpret_cast<float *>(smem_raw);
+  extern __shared__ __align__(128) unsigned char c3_smem[];
+  float *const base = reinterpret_cast<float *>(c3_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float *const wsc = base + warp * P::WARP_FLOATS;
   float2 *const wxf = reinterpret_cast<float2 *>(wsc + P::WXF);
@@ -222,7 +231,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       float v[W];
       // x, scaled by f_j, at the node's offset in the column's box
       const int ox = (loc & 7) - 2 * s0;
-      kb_poly_taps_s<W>(r.x, poly.c[0], v);
+      kb_poly_taps_sym<W>(r.x, poly.c[0], v);
       {
         float4 *dst = reinterpret_cast<float4 *>(wxf + lane * BOXP);
 #pragma unroll
@@ -241,7 +250,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
         }
       }
       const int oy = ((loc >> 3) & 7) - 2 * s1;
-      kb_poly_taps_s<W>(r.y, poly.c[1], v);
+      kb_poly_taps_sym<W>(r.y, poly.c[1], v);
       {
         float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
 #pragma unroll
@@ -259,7 +268,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
         }
       }
       z0 = loc >> 6;
-      kb_poly_taps_s<W>(r.z, poly.c[2], v);
+      kb_poly_taps_sym<W>(r.z, poly.c[2], v);
       {
         // taps at the node's z offset within its aligned pair: a window
         // starting at odd z0 begins in the second half of a pair
@@ -342,7 +351,37 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     __syncwarp();
   }
   __syncthreads();
-  // one vector reduction per non-zero cell of the padded subgrid
+  // ---- write-back.  A tile whose padded box lies inside the grid: the box
+  // goes densely (rows of ZB complex values, the last one zero where EXT is
+  // odd) into the warps' scratch, then one TMA add-reduce adds it to the grid.
+  constexpr int ZB = (EXT + 1) & ~1;
+  static_assert((size_t)EXT * EXT * ZB * 2 <= (size_t)C3_WARPS * P::WARP_FLOATS,
+                "the dense padded tile fits in the warps' scratch");
+  if (use_tma && org[0] + EXT <= g.n[0] && org[1] + EXT <= g.n[1] && org[2] + EXT <= g.n[2] &&
+      (smem_u32(base) & 127u) == 0) {
+    float2 *const stg = reinterpret_cast<float2 *>(base);
+    for (int r = threadIdx.x; r < EXT * EXT; r += C3_THREADS) {
+      const int c0 = r / EXT, c1 = r - c0 * EXT;
+      const float2 *src = sg + c0 * g.sx2 + c1 * g.sy2;
+      float4 *dst = reinterpret_cast<float4 *>(stg + r * ZB);
+#pragma unroll
+      for (int z = 0; z < ZB; z += 2) {
+        const float2 a = src[z];
+        const float2 b = z + 1 < EXT ? src[z + 1] : make_float2(0.f, 0.f);
+        dst[z >> 1] = make_float4(a.x, a.y, b.x, b.y);
+      }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_reduce_add_3d(&gmap, stg, 2 * org[2], org[1], org[0]);
+      bulk_commit();
+      bulk_wait_read_all();  // the scratch stays allocated until the copy has read it
+    }
+    return;
+  }
+  // a tile whose padded box wraps around the grid edge: one vector reduction
+  // per non-zero cell
   for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
     const int c2 = idx % EXT, r = idx / EXT;
     const int c1 = r % EXT, c0 = r / EXT;
@@ -362,8 +401,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
 // nfft_trafo_3d_compute, nfft.c:4020-4265).
 //
 // The nodes of a 2x2x2 sub-cell of a tile share one (W+1)^3 box of the padded
-// subgrid.  A CTA stages its tile's padded subgrid in shared memory (real and
-// imaginary planes), finds where each of the tile's 64 sub-cells starts in the
+// subgrid.  A CTA stages its tile's padded subgrid in shared memory as
+// interleaved complex rows of ZB cells (one TMA copy for a tile whose padded
+// box lies inside the grid, plain loads for one that wraps around the grid
+// edge), finds where each of the tile's 64 sub-cells starts in the
 // item's sorted node range, and its warps take units (at most S3_PM nodes of
 // one sub-cell, a sub-cell's nodes split evenly) from a shared counter:
 //  * lanes evaluate the unit's windows (one lane per node and dimension) into
@@ -384,16 +425,27 @@ struct S3 {
   static constexpr int RPL = 2;
   static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
   static constexpr int WARP_FLOATS = 3 * S3_PM * BOXP;  // wx, wy, wz [S3_PM][BOXP]
-  static constexpr int INTS = 65 + 1;                   // sub-cell starts, task counter
+  static constexpr int ZB = (EXT + 1) & ~1;              // cells of a subgrid row (16-byte rows)
+  // rows per x-plane of the staged subgrid: EXT rounded up to 3 mod 8, so that
+  // a plane is 3 bank groups of 16 bytes (mod 8) past the last but one and a
+  // row of ZB = 18 cells one: box rows (x, y) then fall in bank group
+  // (3x + y) mod 8, and any eight consecutive rows of the lanes' row order
+  // (y fastest, 11 per x) in eight different groups
+  static constexpr int EXTY = EXT + ((11 - EXT % 8) % 8);
+  static constexpr int GRID_CELLS = EXT * EXTY * ZB;     // the padded subgrid [EXT][EXTY][ZB]
+  static constexpr int INTS = 65 + 1;                    // sub-cell starts, task counter
   static_assert(BOXP > BOX, "the x vector needs one zero slot past the box");
+  static_assert(C3_WARPS * WARP_FLOATS * 4 % 128 == 0, "the subgrid starts on a 128-byte boundary");
 };
 
+// warp scratch | subgrid | ints | the TMA barrier (8-byte aligned)
 template <int W>
-inline size_t s3_smem_bytes(const Geom<float> &g)
+__host__ __device__ inline size_t s3_smem_bytes(const Geom<float> &)
 {
   typedef S3<W> P;
-  return ((size_t)C3_WARPS * P::WARP_FLOATS + 2 * (size_t)P::EXT * g.sx) * sizeof(float)
-         + P::INTS * sizeof(int);
+  const size_t b = (size_t)C3_WARPS * P::WARP_FLOATS * sizeof(float) + (size_t)P::GRID_CELLS * sizeof(float2) +
+                   P::INTS * sizeof(int);
+  return (b + 7) / 8 * 8 + sizeof(unsigned long long);
 }
 
 template <int W>
@@ -403,20 +455,22 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
                                                             const uint16_t *__restrict__ sst,
                                                             const uint32_t *__restrict__ perm,
                                                             float2 *__restrict__ f, Geom<float> g,
-                                                            WinPoly poly)
+                                                            WinPoly poly, const __grid_constant__ CUtensorMap gmap,
+                                                            int use_tma)
 {
   typedef S3<W> P;
-  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RPL = P::RPL, PM = S3_PM;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *const base = reinterpret_cast<float *>(smem_raw);
+  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RPL = P::RPL, PM = S3_PM, ZB = P::ZB;
+  extern __shared__ __align__(128) unsigned char c3_smem[];
+  float *const base = reinterpret_cast<float *>(c3_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float *const wx = base + warp * P::WARP_FLOATS;
   float *const wy = wx + PM * BOXP;
   float *const wz = wy + PM * BOXP;
-  float *const sre = base + C3_WARPS * P::WARP_FLOATS;
-  float *const sim = sre + EXT * g.sx;
-  int *const sstart = reinterpret_cast<int *>(sim + EXT * g.sx);
+  float2 *const sgrid = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
+  int *const sstart = reinterpret_cast<int *>(sgrid + P::GRID_CELLS);
   int *const taskctr = sstart + 65;
+  unsigned long long *const bar = reinterpret_cast<unsigned long long *>(
+      c3_smem + (s3_smem_bytes<W>(g) - sizeof(unsigned long long)));
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
@@ -428,23 +482,30 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       rem /= g.ntile[t];
     }
   }
+  // the padded subgrid: one TMA copy where the box lies inside the grid
+  const bool tma = use_tma && org[0] + EXT <= g.n[0] && org[1] + EXT <= g.n[1] && org[2] + EXT <= g.n[2] &&
+                   (smem_u32(sgrid) & 127u) == 0;
   if (threadIdx.x == 0) {
+    if (tma) {
+      mbar_init(bar, 1);
+      mbar_expect_tx(bar, (unsigned)(P::GRID_CELLS * sizeof(float2)));
+      tma_load_3d(sgrid, &gmap, 2 * org[2], org[1], org[0], bar);
+    }
     c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
     c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
   }
-  // stage the padded subgrid; several grid loads in flight per thread
+  if (!tma) {
+    // plain loads (the box wraps around the grid edge); several in flight per thread
 #pragma unroll 4
-  for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
-    const int c2 = idx % EXT, r = idx / EXT;
-    const int c1 = r % EXT, c0 = r / EXT;
-    int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
-    while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
-    while (p1 >= g.n[1]) p1 -= g.n[1];
-    while (p2 >= g.n[2]) p2 -= g.n[2];
-    const float2 v = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
-    const int si = c0 * g.sx + c1 * g.sy + c2;
-    sre[si] = v.x;
-    sim[si] = v.y;
+    for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
+      const int c2 = idx % EXT, r = idx / EXT;
+      const int c1 = r % EXT, c0 = r / EXT;
+      int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
+      while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+      while (p1 >= g.n[1]) p1 -= g.n[1];
+      while (p2 >= g.n[2]) p2 -= g.n[2];
+      sgrid[(c0 * P::EXTY + c1) * ZB + c2] = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
+    }
   }
   // the unused node slots of the weight vectors must hold finite values
   for (int i = lane; i < P::WARP_FLOATS; i += 32) wx[i] = 0.f;
@@ -452,6 +513,14 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
   if (threadIdx.x < 65) sstart[threadIdx.x] = sst[65LL * blockIdx.x + threadIdx.x];
   if (threadIdx.x == 0) *taskctr = 0;
   __syncthreads();
+  if (tma) {
+    // a bounded wait: a copy that never arrives costs this tile, not a hang
+    const bool ok = mbar_wait(bar, 0, TMA_WAIT_POLLS);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicAdd(&g_tma_wait_timeouts, 1ull);
+      return;
+    }
+  }
 
   // units per sub-cell: lane l holds sub-cells 2l and 2l+1
   const int l0 = sstart[2 * lane + 1] - sstart[2 * lane], l1 = sstart[2 * lane + 2] - sstart[2 * lane + 1];
@@ -494,8 +563,8 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       const int loc = (__float_as_int(rj[3]) >> (3 * t)) & 7;
       const int o = loc - (t == 0 ? b0 : (t == 1 ? b1 : b2));
       float v[W];
-      if (poly.same) kb_poly_taps_s<W>(sj, poly.c[0], v);
-      else kb_poly_taps_s<W>(sj, poly.c[t], v);
+      if (poly.same) kb_poly_taps_sym<W>(sj, poly.c[0], v);
+      else kb_poly_taps_sym<W>(sj, poly.c[t], v);
       float *dst = wx + (t * PM + j) * BOXP;
       float e[BOXP];
 #pragma unroll
@@ -510,7 +579,6 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
     }
     __syncwarp();
 
-    const int sbase = b0 * g.sx + b1 * g.sy + b2;
     float acc[2 * PM];
 #pragma unroll
     for (int j = 0; j < 2 * PM; ++j) acc[j] = 0.f;
@@ -526,22 +594,21 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
         const int bx = rr / BOX;
         by[qq] = rr - bx * BOX;
         wbx[qq] = ok ? bx : BOXP - 1;  // rows past the box take the zero slot of the x vector
-        const float *pr = sre + sbase + bx * g.sx + by[qq] * g.sy;
-        const float *pi = sim + sbase + bx * g.sx + by[qq] * g.sy;
-        // row starts are even (even plane strides, even sub-cell z origin):
-        // pairs of z values load as 8-byte words
+        // rows of ZB (even) cells from an even sub-cell z origin start on a
+        // 16-byte boundary: two complex values per load
+        const float2 *pr = sgrid + ((b0 + bx) * P::EXTY + (b1 + by[qq])) * ZB + b2;
 #pragma unroll
         for (int z = 0; z + 1 < BOX; z += 2) {
-          const float2 a = *reinterpret_cast<const float2 *>(pr + z);
-          const float2 b = *reinterpret_cast<const float2 *>(pi + z);
+          const float4 a = *reinterpret_cast<const float4 *>(pr + z);
           gr[qq][z] = a.x;
-          gr[qq][z + 1] = a.y;
-          gi[qq][z] = b.x;
-          gi[qq][z + 1] = b.y;
+          gi[qq][z] = a.y;
+          gr[qq][z + 1] = a.z;
+          gi[qq][z + 1] = a.w;
         }
         if (BOX & 1) {
-          gr[qq][BOX - 1] = pr[BOX - 1];
-          gi[qq][BOX - 1] = pi[BOX - 1];
+          const float2 a = pr[BOX - 1];
+          gr[qq][BOX - 1] = a.x;
+          gi[qq][BOX - 1] = a.y;
         }
       }
 #pragma unroll

@@ -8,9 +8,39 @@
 // (17 entries) and of every 2x2x2 sub-cell (65 entries) within the item's
 // node range is kept, so the transform kernels need no pass over the nodes to
 // find them.
+#include <mutex>
+
 #include "gb_internal.h"
 
 namespace gb {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ext_y)
+{
+  static std::once_flag once;
+  static EncodeTiledFn enc = nullptr;
+  std::call_once(once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      enc = (EncodeTiledFn)fn;
+  });
+  // rows of 2 n_2 floats must be 16-byte multiples, the box within 256 per dimension
+  const int zb = (ext + 1) & ~1;
+  if (!enc || !grid || (n[2] & 1) || ext > 256 || ext_y > 256 || 2 * zb > 256) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * n[2], (cuuint64_t)n[1], (cuuint64_t)n[0]};
+  const cuuint64_t strides[2] = {(cuuint64_t)8 * n[2], (cuuint64_t)8 * n[2] * n[1]};
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * zb), (cuuint32_t)ext_y, (cuuint32_t)ext};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, grid, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 __global__ void k_c3_records(const float *__restrict__ xs, Geom<float> g, float4 *__restrict__ rec)
 {

@@ -176,6 +176,34 @@ __device__ __forceinline__ void kb_poly_taps_s(float s, const float (&c)[KB_POLY
   }
 }
 
+// The same W taps from the window's symmetry: tap W-1-l at s equals tap l at
+// -s (the Kaiser-Bessel window is even and the taps are symmetric about the
+// window centre), so with P_l(s) = E_l(s^2) + s O_l(s^2) split into its even
+// and odd powers, taps l and W-1-l are E_l + s O_l and E_l - s O_l: two
+// degree-4 Horner chains in s^2 per pair of taps (10 multiply-adds instead of
+// 18), from the coefficients of the first W/2 taps only.
+template <int W>
+__device__ __forceinline__ void kb_poly_taps_sym(float s, const float (&c)[KB_POLY_WMAX][KB_POLY_DP], float (&v)[W])
+{
+  static_assert(W <= KB_POLY_WMAX && W % 2 == 0, "even width with a polynomial form");
+  static_assert(KB_POLY_DP == 10, "degree-9 form: five even and five odd coefficients");
+  const float t = s * s;
+#pragma unroll
+  for (int l = 0; l < W / 2; ++l) {
+    float e = c[l][8], o = c[l][9];
+    e = fmaf(e, t, c[l][6]);
+    o = fmaf(o, t, c[l][7]);
+    e = fmaf(e, t, c[l][4]);
+    o = fmaf(o, t, c[l][5]);
+    e = fmaf(e, t, c[l][2]);
+    o = fmaf(o, t, c[l][3]);
+    e = fmaf(e, t, c[l][0]);
+    o = fmaf(o, t, c[l][1]);
+    v[l] = fmaf(s, o, e);
+    v[W - 1 - l] = fmaf(-s, o, e);
+  }
+}
+
 // double precision: the W taps of a node from the degree-16 form
 template <int W>
 __device__ __forceinline__ void kb_polyd_taps_s(double s, const double (&c)[KB_POLY_WMAX][KB_POLYD_DP],

@@ -1,6 +1,7 @@
 // gb_internal.h -- host-side interfaces between the library's translation units.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (type only; the encoder comes through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
@@ -79,7 +80,21 @@ struct Col3Bufs {
   const float4 *rec;    // per sorted node: s_0, s_1, s_2, packed window starts in the tile
   const uint16_t *cst;  // per work item: 17 column starts
   const uint16_t *sst;  // per work item: 65 sub-cell starts
+  // TMA views of the oversampled grid as f32 [n_0][n_1][2 n_2] with a box of
+  // the padded tile: ext x ext_y x 2 zb floats, zb = ext rounded up to even;
+  // B^T's with ext_y = ext, B's with ext_y = S3<w>::EXTY (see gb_col3.cuh).
+  // Null where they could not be encoded (the kernels then use plain loads).
+  const CUtensorMap *grid_map;
+  const CUtensorMap *grid_map_b;
 };
+// Encodes such a view for a plan's grid (false: not representable, e.g. an
+// odd n_2, whose rows are not 16-byte multiples).
+bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ext_y);
+// y extent of B's staged subgrid for window width w (3-D single precision)
+int col3_b_ext_y(int w);
+// Device-side wait time-outs recorded since the last call (bounded waits on
+// TMA copies; non-zero means a copy did not arrive and the kernel gave up).
+unsigned long long read_wait_timeouts();
 void launch_c3_setup(const float *xs, const Geom<float> &g, const WorkItem *items, int nitems,
                      const uint32_t *keys, float4 *rec, uint16_t *cst, uint16_t *sst, cudaStream_t s);
 int group3_max_item();
@@ -95,8 +110,11 @@ void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid
 // column of CX x-cells by 8 y-cells)); col2_column_width(w) = CX, 0 where
 // the width has no such kernel
 int col2_column_width(int w);
+// grid_lo non-null: the compensated form (B^T's rounding errors gathered in
+// grid_lo, n_0 n_1 complex, zeroed by the caller, then folded into grid)
 void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
-                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
+                    const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s,
+                    float2 *grid_lo = nullptr);
 void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
                    float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
 // the B^T of the same layout in double precision, and a per-node B on the
@@ -128,6 +146,8 @@ struct PlanViewF {
   bool col2;           // nodes keyed by 2-D column (the column kernels apply)
   const WinPoly *poly; // the plan's polynomial window (host copy)
   cudaStream_t stream;
+  Col3Bufs c3;         // node records of the 3-D single-precision kernels (null elsewhere)
+  float2 *grid;        // the oversampled grid
 };
 bool plan_view_f(void *nfftf_plan_ptr, PlanViewF *v);
 // re-bin a 2-D plan's nodes on tiles of edge T (8, 16 or 32), or with T = 0

@@ -73,9 +73,14 @@ struct Ctx {
   WinPoly poly = {};     // polynomial window of the single-precision 2-D / 3-D kernels
   WinPolyD polyd = {};   // the same in double precision (2-D double-precision kernels)
   bool col2 = false;     // 2-D column kernels (nodes keyed by column)
+  int comp = -1;         // compensated 2-D single-precision B^T: 1 on, 0 off, -1 the default (on for m >= 6)
+  void *grid_lo = nullptr;  // its error grid (n_total complex), allocated on first use
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
+  CUtensorMap grid_map;      // TMA views of `grid` for the 3-D column kernels (B^T, B)
+  CUtensorMap grid_map_b;
+  bool grid_map_ok = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // FFT: one plan for d <= 3; for d > 3 a rank-3 plan over the last three
@@ -435,6 +440,8 @@ static void init_help(typename Api<R>::plan *ths)
       dev_alloc<R>((void **)&c->c3rec, M * sizeof(float4));
       dev_alloc<R>((void **)&c->c3cst, cap * 17 * sizeof(uint16_t));
       dev_alloc<R>((void **)&c->c3sst, cap * 65 * sizeof(uint16_t));
+      c->grid_map_ok = encode_grid_map(&c->grid_map, c->grid, g.n, g.ext[0], g.ext[0]) &&
+                       encode_grid_map(&c->grid_map_b, c->grid, g.n, g.ext[0], col3_b_ext_y(g.w));
     }
     make_fft<R>(c);
   }
@@ -572,6 +579,8 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   b.rec = c->c3rec;
   b.cst = c->c3cst;
   b.sst = c->c3sst;
+  b.grid_map = c->grid_map_ok ? &c->grid_map : nullptr;
+  b.grid_map_b = c->grid_map_ok ? &c->grid_map_b : nullptr;
   return b;
 }
 
@@ -613,9 +622,15 @@ template <typename R>
 static bool bt2_stage(Ctx<R> *c, const typename Cx<R>::T *f)
 {
   if (!c->col2) return false;
-  if constexpr (std::is_same<R, float>::value)
-    launch_bt2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
-  else
+  if constexpr (std::is_same<R, float>::value) {
+    float2 *lo = nullptr;
+    if (c->comp == 1 || (c->comp < 0 && c->g.m >= 6)) {
+      if (!c->grid_lo) dev_alloc<R>(&c->grid_lo, (size_t)c->g.n_total * sizeof(float2));
+      lo = (float2 *)c->grid_lo;
+      GB_CUDA(cudaMemsetAsync(lo, 0, (size_t)c->g.n_total * sizeof(float2), c->stream));
+    }
+    launch_bt2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream, lo);
+  } else
     launch_bt2_col_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->polyd, c->stream);
   return true;
 }
@@ -865,6 +880,7 @@ static void finalize(typename Api<R>::plan *ths)
     cudaFree(c->xs);
     cudaFree(c->perm);
     cudaFree(c->grid);
+    cudaFree(c->grid_lo);
     cudaFree(c->fhat_dev);
     cudaFree(c->f_dev);
     cudaFree(c->cphi);
@@ -932,6 +948,17 @@ static void init_default(typename Api<R>::plan *ths, int d, int *N, int M, int m
 }
 
 // ------------------------------------------------------------ extensions
+// mode 1 / 0 / -1 (default: on for m >= 6) for the compensated single-precision
+// 2-D column B^T; -1 returned where the plan runs no such kernel
+template <typename R>
+static int set_compensated(typename Api<R>::plan *ths, int mode)
+{
+  Ctx<R> *c = ctx_of<R>(ths);
+  if (!std::is_same<R, float>::value || c->g.d != 2 || c->direct || !c->col2 || mode < -1 || mode > 1) return -1;
+  c->comp = mode;
+  return 0;
+}
+
 template <typename R>
 static int set_stream(typename Api<R>::plan *ths, void *stream)
 {
@@ -1013,6 +1040,7 @@ extern "C" {
   const char *X##check(X##plan *ths) { return check<R>(ths); }                                     \
   void X##finalize(X##plan *ths) { finalize<R>(ths); }                                             \
   int X##gb_set_stream(X##plan *ths, void *stream) { return set_stream<R>(ths, stream); }          \
+  int X##gb_set_compensated(X##plan *ths, int mode) { return set_compensated<R>(ths, mode); }      \
   void *X##gb_get_stream(X##plan *ths) { return (void *)ctx_of<R>(ths)->stream; }                  \
   void *X##gb_device_f_hat(X##plan *ths) { return (void *)ctx_of<R>(ths)->fhat_dev; }              \
   void *X##gb_device_f(X##plan *ths) { return (void *)ctx_of<R>(ths)->f_dev; }                     \
@@ -1092,6 +1120,8 @@ bool plan_view_f(void *pp, PlanViewF *v)
   v->col2 = c->col2;
   v->poly = &c->poly;
   v->stream = c->stream;
+  v->c3 = col3_bufs<float>(c);
+  v->grid = c->grid;
   return true;
 }
 

@@ -26,6 +26,7 @@
 
 #include "../../include/nfft3.h"
 #include "gb_common.cuh"
+#include "gb_internal.h"
 
 namespace {
 
@@ -157,6 +158,11 @@ extern "C" {
 
 GB_MALLOC_API(nfft_, "nfft_malloc")
 GB_MALLOC_API(nfftf_, "nfftf_malloc")
+
+unsigned long long nfft_gb_tma_wait_timeouts(void)
+{
+  return gb::read_wait_timeouts();
+}
 
 const char *nfft_gb_last_error(void)
 {

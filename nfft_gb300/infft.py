@@ -25,11 +25,22 @@ def _ext(lib, name, restype, argtypes):
     return fn
 
 
+def disk_damping(N):
+    """Damping factors w_hat of the reference's MRI reconstruction
+    (applications/mri/mri2d/reconstruct_data_2d.c: CGNR | PRECOMPUTE_DAMP):
+    1 on the image's inscribed disk (pixel (j, k), j2 = j - N/2, k2 = k - N/2,
+    sqrt(j2^2 + k2^2) <= N/2), 0 outside."""
+    j = np.arange(N) - N // 2
+    r = np.sqrt(j[:, None] ** 2 + j[None, :] ** 2)
+    return (r <= N / 2).astype(np.float64).reshape(-1)
+
+
 class CGNR:
     """CGNR on one plan; weights w (M) make it the weighted normal equations
-    A^H W A f = A^H W y (PRECOMPUTE_WEIGHT)."""
+    A^H W A f = A^H W y (PRECOMPUTE_WEIGHT); damping factors w_hat (N_total)
+    enter as the reference's PRECOMPUTE_DAMP."""
 
-    def __init__(self, lib, single, N, x, m, y, w=None, refresh=0, cgne=False):
+    def __init__(self, lib, single, N, x, m, y, w=None, refresh=0, cgne=False, w_hat=None):
         self.lib = lib
         self.single = single
         M = len(x)
@@ -40,10 +51,14 @@ class CGNR:
         flags = abi.CGNE if cgne else abi.CGNR
         if w is not None:
             flags |= abi.PRECOMPUTE_WEIGHT
+        if w_hat is not None:
+            flags |= abi.PRECOMPUTE_DAMP
         self.solver = Solver(self.plan, flags)
         self.solver.y[:] = y
         if w is not None:
             self.solver.w[:] = w
+        if w_hat is not None:
+            self.solver.w_hat[:] = w_hat
         self.solver.f_hat_iter[:] = 0
         pfx = "solverf_" if single else "solver_"
         self._set_sync = _ext(lib, pfx + "gb_set_sync", C.c_int, [C.c_void_p, C.c_int])
@@ -88,9 +103,9 @@ class CGNR:
         self.plan.finalize()
 
 
-def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14):
+def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14, w_hat=None):
     """FP64 CGNR run to convergence (relative change of f below rtol)."""
-    s = CGNR(lib, False, N, x, m, y, w=w)
+    s = CGNR(lib, False, N, x, m, y, w=w, w_hat=w_hat)
     s.set_sync(1)
     s.before_loop()
     prev = s.f_hat.copy()
@@ -108,11 +123,11 @@ def fp64_solution(lib, N, x, m, y, w=None, max_iter=3000, rtol=1e-14):
     return out, it
 
 
-def run_iterations(lib, single, N, x, m, y, iters, w=None, refresh=0):
+def run_iterations(lib, single, N, x, m, y, iters, w=None, refresh=0, w_hat=None):
     """Run `iters` CGNR steps timed (enqueued back to back, one host
     synchronisation); returns (f_hat_iter after the last step, seconds,
     per-step dot_r)."""
-    s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0)
+    s = CGNR(lib, single, N, x, m, y, w=w, refresh=refresh if single else 0, w_hat=w_hat)
     s.set_sync(0)
     t0 = time.perf_counter()
     s.before_loop()

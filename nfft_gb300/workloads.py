@@ -3,6 +3,9 @@
 The reference has no public benchmark data set; these stand in with the shapes
 and value distributions of the workloads the benchmark is quoted on:
 
+* uniform or clustered nodes on the d-torus: iid U[-1/2, 1/2)^d, or a
+  mixture of 32 isotropic Gaussians (centres uniform, std 0.02) wrapped to
+  the torus;
 * radial k-space: `spokes` spokes at angles pi*s/spokes, `samples` radial
   positions uniformly spaced in [-1/2, 1/2);
 * interleaved Archimedean spirals: arm a, t in [0, 1): r = 0.5 t,
@@ -12,6 +15,20 @@ and value distributions of the workloads the benchmark is quoted on:
   vector f_hat of the NFFT in natural order.
 """
 import numpy as np
+
+
+def cube_nodes(M, d, dist="uniform", seed=0, dtype=np.float32):
+    """M nodes in [-1/2, 1/2)^d: "uniform" or "clustered" (32 Gaussians, std 0.02)."""
+    rng = np.random.default_rng(seed)
+    if dist == "uniform":
+        return rng.uniform(-0.5, 0.5, size=(M, d)).astype(dtype)
+    if dist != "clustered":
+        raise ValueError("unknown node distribution %r" % dist)
+    c = rng.uniform(-0.5, 0.5, size=(32, d))
+    x = c[rng.integers(0, 32, M)] + 0.02 * rng.standard_normal((M, d))
+    x = (((x + 0.5) % 1.0) - 0.5).astype(dtype)
+    x[x >= 0.5] = -0.5
+    return x
 
 
 def radial_nodes(spokes=402, samples=512):

@@ -1,5 +1,6 @@
 """The reference's own single-precision error at the 3-D benchmark shape
-(N = 128^3, n = 256^3, m = 4, Kaiser-Bessel), and at the 2-D radial shape of
+(N = 128^3, n = 256^3, m = 4, Kaiser-Bessel; uniform nodes, and nodes
+clustered as a mixture of 32 Gaussians of std 0.02), and at the 2-D radial shape of
 the inverse-NFFT workload (N = 256^2, n = 512^2, m = 6): nfftf_trafo and nfftf_adjoint
 of the reference compiled in place (oracle/ref/Makefile, single-precision
 FFT stand-in) on a 4096-node subset plan with seeded inputs, stored as
@@ -43,6 +44,20 @@ def inputs():
     return x, fh, f, idx
 
 
+def inputs_clustered():
+    """The 3-D shape again, the 4096 nodes drawn from the clustered
+    distribution of the benchmark's second variant (32 Gaussians, std 0.02,
+    wrapped to the torus)."""
+    from nfft_gb300 import workloads
+    x = workloads.cube_nodes(M, 3, "clustered", SEED + 2)
+    rng = np.random.default_rng(SEED + 3)
+    NN = int(np.prod(N))
+    fh = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
+    idx = np.sort(rng.choice(NN, NSAMP, replace=False))
+    return x, fh, f, idx
+
+
 def inputs_radial():
     """The same for the 2-D radial shape."""
     from nfft_gb300 import workloads
@@ -75,6 +90,8 @@ def main():
         sys.exit("reference library not built (oracle.build_reference())")
     x2, fh2, f2, idx2 = inputs_radial()
     f_ref2, fhat_ref2 = run(ref, True, N2, n2, m2, x2, fh2, f2, idx2)
+    x3, fh3, f3, idx3 = inputs_clustered()
+    f_ref3, fhat_ref3 = run(ref, True, N, n, m, x3, fh3, f3, idx3)
     x, fh, f, idx = inputs()
     p = Plan(ref, True, N, M, n=n, m=m, flags=FLAGS)
     p.x[:] = x
@@ -87,7 +104,8 @@ def main():
     fhat_ref = p.f_hat[idx].copy()
     p.finalize()
     np.savez_compressed(os.path.join(HERE, "cfg2_single_ref.npz"), f_ref=f_ref, fhat_ref=fhat_ref, idx=idx,
-                        radial_f_ref=f_ref2, radial_fhat_ref=fhat_ref2, radial_idx=idx2)
+                        radial_f_ref=f_ref2, radial_fhat_ref=fhat_ref2, radial_idx=idx2,
+                        clustered_f_ref=f_ref3, clustered_fhat_ref=fhat_ref3, clustered_idx=idx3)
     print("cfg2_single_ref.npz written")
 
 

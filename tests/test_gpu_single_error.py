@@ -58,6 +58,37 @@ def test_fp32_error_within_twice_the_reference_nfftf(gpulib):
     assert e_gpu_a <= 2 * e_ref_a, (e_gpu_a, e_ref_a)
 
 
+def _subset_errors(lib, z, key, Nc, nc, mc, x, fh, f, idx):
+    """Relative l2 errors of the reference's nfftf (fixture) and of this
+    library's FP32 plan, both against the FP64 NDFT on the GPU."""
+    assert np.array_equal(idx, z[key + "_idx"])
+    f_gpu, fhat_gpu = G.run(lib, True, Nc, nc, mc, x, fh, f, idx)
+    q = Plan(lib, False, Nc, len(x), n=nc, m=mc, flags=G.FLAGS)
+    q.x[:] = x.astype(np.float64)
+    q.f_hat[:] = fh.astype(np.complex128)
+    q.trafo_direct()
+    f_ndft = q.f.copy()
+    q.f[:] = f.astype(np.complex128)
+    q.adjoint_direct()
+    fhat_ndft = q.f_hat[idx].copy()
+    q.finalize()
+    return (rel(z[key + "_f_ref"], f_ndft), rel(f_gpu, f_ndft),
+            rel(z[key + "_fhat_ref"], fhat_ndft), rel(fhat_gpu, fhat_ndft))
+
+
+def test_fp32_error_clustered_within_twice_the_reference_nfftf(gpulib):
+    """The 3-D benchmark shape with clustered nodes (the second variant of the
+    3-D workload: 32 Gaussians of std 0.02, which crowd many nodes into the
+    same cells): 4096 such nodes, N = 128^3, n = 256^3, m = 4."""
+    z = np.load(os.path.join(HERE, "golden", "cfg2_single_ref.npz"))
+    x, fh, f, idx = G.inputs_clustered()
+    e_ref_t, e_gpu_t, e_ref_a, e_gpu_a = _subset_errors(gpulib, z, "clustered", G.N, G.n, G.m, x, fh, f, idx)
+    print("clustered 3-D trafo: reference nfftf %.2e, this library %.2e; adjoint: reference %.2e, "
+          "this library %.2e" % (e_ref_t, e_gpu_t, e_ref_a, e_gpu_a))
+    assert e_gpu_t <= 2 * e_ref_t, (e_gpu_t, e_ref_t)
+    assert e_gpu_a <= 2 * e_ref_a, (e_gpu_a, e_ref_a)
+
+
 def test_fp32_error_radial_2d_within_twice_the_reference_nfftf(gpulib):
     """The same at the 2-D radial shape of the inverse-NFFT workload (the
     column kernels): 4096 of its nodes, N = 256^2, n = 512^2, m = 6."""

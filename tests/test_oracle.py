@@ -97,6 +97,23 @@ def test_oracle_solver_vs_reference_run(refrun):
         s.close()
 
 
+def test_oracle_vs_reference_run_full_2d_fp64_shape():
+    """The oracle at the full 2-D FP64 shape (N = 256^2, n = 512^2, m = 6,
+    M = 65536) against the reference run stored in tests/golden/cfg1_ref.npz."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_cfg1_ref as G1
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cfg1_ref.npz"))
+    x, fh, y = G1.inputs()
+    assert G1.sha(x, fh, y) == str(z["inputs_sha256"])
+    o = oracle.OraclePlan(G1.N, G1.M, n=G1.n, m=G1.m)
+    o.set_nodes(x)
+    o.precompute()
+    assert rel_l2(o.trafo(fh), z["trafo"]) < 1e-14
+    assert rel_l2(o.adjoint(y), z["adjoint"]) < 1e-14
+    assert G1.sha(o.index_x()) == str(z["index_x_sha256"])
+
+
 def test_oracle_fft_matches_numpy():
     rng = np.random.default_rng(1)
     for shape in [(16,), (12,), (8, 32), (4, 8, 16), (6, 10)]:

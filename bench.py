@@ -96,7 +96,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -438,10 +438,13 @@ def run_gpu(args, wl):
 def run_infft(args):
     """Mixed-precision inverse NFFT on 2-D radial k-space: N = 256^2, sigma = 2,
     m = 6, 402 spokes x 512 samples, 20-ellipse phantom (seed 1), y = A f_true
-    (FP64 transform) + complex Gaussian noise at 40 dB SNR.  K CGNR iterations
-    in FP32 with FP64 inner products and an FP64 residual refresh every 10
-    iterations; reported: wall time (value), distance to the FP64 CGNR iterate
-    after the same K iterations, and the error against f_true for each."""
+    (FP64 transform) + complex Gaussian noise at 40 dB SNR.  K CGNR steps per
+    solver -- FP64; FP32 transforms with FP64 inner products; the same with an
+    FP64 residual refresh every 10 steps -- enqueued back to back and timed
+    (value: the FP32 solver's time); reported per solver: ms per step, the
+    error against f_true after K steps and its smallest value over the steps
+    (noisy data: CGNR semi-converges), the distance to the FP64 solver's
+    iterate, and the true data residual (FP64 transform)."""
     import torch
     import nfft_gb300
     from nfft_gb300 import infft, workloads
@@ -460,26 +463,100 @@ def run_infft(args):
     y = workloads.add_noise(p.f.copy(), 40.0, np.random.default_rng(1))
     p.finalize()
     nt = np.linalg.norm(f_true)
+    solvers = {"fp64": (False, 0), "fp32": (True, 0), "fp32_refresh10": (True, 10)}
+    if args.solver != "all":
+        solvers = {args.solver: solvers[args.solver]}
     runs = {}
-    for name, single, refresh in (("fp64", False, 0), ("fp32_fp64dots_refresh10", True, 10),
-                                  ("fp32_fp64dots_norefresh", True, 0)):
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    for name, (single, refresh) in solvers.items():
         infft.run_iterations(lib, single, N, x, m, y, 3, refresh=refresh)  # warm-up
         f, sec, dots = infft.run_iterations(lib, single, N, x, m, y, K, refresh=refresh)
-        runs[name] = dict(f=f, seconds=sec, dot_r=dots[-1])
-    f64 = runs["fp64"]["f"]
+        runs[name] = dict(f=f, seconds=sec)
+    clk = clocks.stop()
+    res = infft.TrueResidual(lib, N, x, m, y)
     out = {}
-    for name, r in runs.items():
-        out[name] = {"seconds": r["seconds"], "ms_per_iter": 1e3 * r["seconds"] / K,
+    for name, (single, refresh) in solvers.items():
+        # the error trajectory over the steps (untimed: 10 steps at a time)
+        s = infft.CGNR(lib, single, N, x, m, y, refresh=refresh)
+        s.set_sync(0)
+        s.before_loop()
+        errs = []
+        for _ in range(K // 10):
+            s.steps(10)
+            s.sync()
+            errs.append(float(np.linalg.norm(s.f_hat - f_true) / nt))
+        s.close()
+        r = runs[name]
+        out[name] = {"seconds": r["seconds"], "ms_per_step": 1e3 * r["seconds"] / K,
                      "rel_err_vs_f_true": float(np.linalg.norm(r["f"] - f_true) / nt),
-                     "rel_dist_to_fp64_iterate": float(np.linalg.norm(r["f"] - f64) / np.linalg.norm(f64)),
-                     "dot_r": r["dot_r"]}
-    mixed = out["fp32_fp64dots_refresh10"]
-    line = {"metric": "iNFFT CGNR wall time for K iterations, 2-D radial (FP32 + FP64 dots/refresh)",
-            "value": mixed["seconds"], "unit": "s", "n_gpus": 1, "higher_is_better": False,
-            "dtype": "f32 (FP64 dots, FP64 residual refresh every 10)", "data": "synthetic",
+                     "min_rel_err_vs_f_true": min(errs) if errs else None,
+                     "true_rel_residual": res(r["f"])}
+        if "fp64" in runs:
+            f64 = runs["fp64"]["f"]
+            out[name]["rel_dist_to_fp64_iterate"] = float(np.linalg.norm(r["f"] - f64) / np.linalg.norm(f64))
+    res.close()
+    head = "fp32" if "fp32" in out else next(iter(out))
+    line = {"metric": "iNFFT CGNR wall time for K steps, 2-D radial (FP32 transforms, FP64 inner products)",
+            "value": out[head]["seconds"], "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f32 (FP64 inner products)", "data": "synthetic",
             "config": {"workload": "2-D radial iNFFT N=256^2 n=512^2 m=6 402x512 spokes, 20 ellipses, 40 dB",
                        "M": M, "solver": "CGNR", "iterations": K},
-            "runs": out}
+            "clocks": clk, "runs": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_convergence(args):
+    """Where CGNR gets on the spiral trajectory of the learned workload (one
+    trajectory, noiseless data, 20-ellipse phantom): for the FP64 solver, the
+    FP32 solver with FP64 inner products and the same with an FP64 residual
+    refresh every 10 steps, unweighted and with the fixed-point weights, every
+    10 steps the true relative data residual (FP64 transform), the relative
+    image error against the phantom and the image error in the band
+    |nu| <= 0.45 the samples determine; reported: the steps to a 1e-5 residual
+    and the smallest errors reached within --iters steps (unweighted; half as
+    many with weights)."""
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import dcf, infft, workloads
+    from nfft_gb300.plan import Plan
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lib = nfft_gb300.lib()
+    N, m = [256, 256], 6
+    x = dcf.spiral(1000, 16, 8192)
+    f_true = workloads.ellipse_phantom(256, 20, seed=1000)
+    p = Plan(lib, False, N, len(x), n=[512, 512], m=m, flags=infft.PLAN_FLAGS)
+    p.x[:] = x
+    p.precompute_one_psi()
+    p.f_hat[:] = f_true
+    p.trafo()
+    y = p.f.copy()
+    p.finalize()
+    res = infft.TrueResidual(lib, N, x, m, y)
+    wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
+    out = {}
+    for wname, w, total in (("unweighted", None, args.iters), ("fixed_point_weights", wfp, args.iters // 2)):
+        for sname, single, refresh in (("fp64", False, 0), ("fp32", True, 0), ("fp32_refresh10", True, 10)):
+            s = infft.CGNR(lib, single, N, x, m, y, w=w, refresh=refresh)
+            s.set_sync(0)
+            s.before_loop()
+            rows = []
+            for k in range(total // 10):
+                s.steps(10)
+                s.sync()
+                f = s.f_hat
+                rows.append(((k + 1) * 10, res(f)) + infft.image_errors(f, f_true))
+            s.close()
+            a = np.array(rows)
+            out["%s/%s" % (wname, sname)] = {
+                "steps_to_resid_1e-5": next((int(r[0]) for r in rows if r[1] < 1e-5), None),
+                "min_resid": float(a[:, 1].min()), "min_image_err": float(a[:, 2].min()),
+                "min_band_err": float(a[:, 3].min()), "steps": total}
+    res.close()
+    line = {"metric": "CGNR convergence on one spiral trajectory (2-D, N=256^2, m=6, noiseless)",
+            "value": out["unweighted/fp32"]["steps_to_resid_1e-5"], "unit": "steps", "n_gpus": 1,
+            "higher_is_better": False, "data": "synthetic", "runs": out}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -529,8 +606,11 @@ def run_batched(args):
     classes = b.autotune(reps=3)
     t_tune = time.perf_counter() - t0
     b.time(args.warmup, 1)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     ms_stream = b.time(reps, 0)
-    ms_graph = b.time(reps, 1)
+    ms_graph = b.time(max(reps, 50), 1)
+    clk = clocks.stop()
     cfgs = {}
     for k in range(len(plans)):
         cfgs.setdefault("%s" % (b.config(k),), 0)
@@ -544,7 +624,7 @@ def run_batched(args):
             "ms_per_round": {"graph_autotuned": ms_graph, "stream_autotuned": ms_stream,
                              "graph_untuned": ms_graph_untuned, "stream_untuned": ms_stream_untuned,
                              "one_plan_at_a_time_own_streams": t_seq * 1e3},
-            "speedup_vs_one_at_a_time": t_seq * 1e3 / ms_graph,
+            "speedup_vs_one_at_a_time": t_seq * 1e3 / ms_graph, "clocks": clk,
             "autotune": {"classes": classes, "seconds": t_tune, "chosen_T_tpn_counts": cfgs},
             "setup_s": t_setup}
     b.close()
@@ -579,11 +659,13 @@ def run_learned(args):
     2 pi (24 t + a/16) + random rotation, radius jitter 1e-4).  The MLP is
     trained on `--train` seeded trajectories against 20 fixed-point iterations
     w <- w/|A A^H w|; on `--test` held-out trajectories with ellipse phantoms
-    (noiseless data) FP32 CGNR (FP64 dots, FP64 residual refresh) with the
-    learned weights, with the fixed-point weights and unweighted are run until
-    the relative data residual ||y - A f|| / ||y|| falls below 1e-5 (the
-    reference's own stopping rule is on its residual); value = median wall
-    time with the learned weights."""
+    (noiseless data) FP32 CGNR (FP64 inner products) runs with the learned
+    weights, with the fixed-point weights and unweighted until the true
+    relative data residual ||y - A f|| / ||y|| (A the FP64 transform) falls
+    below 1e-5.  value = median wall time with the learned weights, their
+    inference (features + network) included; the image errors at that point
+    (whole image, and the band |nu| <= 0.45 the samples determine) are
+    reported beside it."""
     import torch
     import nfft_gb300
     from nfft_gb300 import dcf, infft, workloads
@@ -608,6 +690,8 @@ def run_learned(args):
     t_train = time.perf_counter() - t0
     del feat, target
     rows = []
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     for i in range(args.test):
         x = dcf.spiral(1000 + i, arms, samples)
         f_true = workloads.ellipse_phantom(256, 20, seed=1000 + i)
@@ -618,33 +702,41 @@ def run_learned(args):
         p.trafo()
         y = p.f.copy()
         p.finalize()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         w = net.weights(lib, x, n).cpu().numpy()
         t_w = time.perf_counter() - t0
         wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
         row = {"weights_s": t_w}
         for name, ww in (("plain", None), ("learned", w), ("fixed_point", wfp)):
-            r = infft.time_to_tolerance(lib, True, N, x, m, y, None, tol=1e-5, w=ww, refresh=10,
-                                        max_iter=args.max_iter, criterion="residual")
+            r = infft.time_to_tolerance(lib, True, N, x, m, y, tol=1e-5, w=ww, max_iter=args.max_iter)
             f = r.pop("f")
-            r["rel_err_vs_f_true"] = float(np.linalg.norm(f - f_true) / np.linalg.norm(f_true))
+            r["rel_err_vs_f_true"], r["band_err_vs_f_true"] = infft.image_errors(f, f_true)
+            if name == "learned":
+                r["seconds_with_inference"] = r["seconds"] + t_w
             row[name] = r
         rows.append(row)
+    clk = clocks.stop()
 
     def med(name, key):
         return float(np.median([r[name][key] for r in rows]))
 
-    line = {"metric": "iNFFT time to 1e-5 relative residual: learned vs plain (2-D spirals)",
-            "value": med("learned", "seconds"), "unit": "s", "n_gpus": 1, "higher_is_better": False,
-            "dtype": "f32 (FP64 dots, FP64 residual refresh every 10)", "data": "synthetic",
+    line = {"metric": "iNFFT time to 1e-5 relative data residual: learned vs plain (2-D spirals)",
+            "value": med("learned", "seconds_with_inference"), "unit": "s", "n_gpus": 1,
+            "higher_is_better": False, "dtype": "f32 (FP64 inner products)", "data": "synthetic",
             "config": {"workload": "2-D spiral iNFFT N=256^2 n=512^2 m=6, 16 arms x 8192, MLP 8-64-64-1",
                        "train_trajectories": args.train, "test_trajectories": args.test,
-                       "epochs": args.epochs},
-            "median": {k: {"seconds": med(k, "seconds"), "iters": med(k, "iters")}
+                       "epochs": args.epochs, "criterion": "||y - A f|| / ||y|| < 1e-5, A in FP64, "
+                       "checked every 5 steps"},
+            "clocks": clk,
+            "median": {k: {"seconds": med(k, "seconds"), "iters": med(k, "iters"),
+                           "rel_err_vs_f_true": med(k, "rel_err_vs_f_true"),
+                           "band_err_vs_f_true": med(k, "band_err_vs_f_true")}
                        for k in ("plain", "learned", "fixed_point")},
             "reached": {k: int(sum(r[k]["reached"] for r in rows)) for k in ("plain", "learned", "fixed_point")},
-            "speedup_learned_vs_plain": med("plain", "seconds") / max(med("learned", "seconds"), 1e-12),
-            "training": {"data_s": t_data, "train_s": t_train, "loss_first": hist[0], "loss_last": hist[-1]},
+            "speedup_learned_vs_plain": med("plain", "seconds") / max(med("learned", "seconds_with_inference"), 1e-12),
+            "training": {"data_s": t_data, "train_s": t_train, "loss_first": hist[0], "loss_last": hist[-1],
+                         "loss_per_epoch": hist},
             "weights_inference_s_median": float(np.median([r["weights_s"] for r in rows])),
             "per_trajectory": rows}
     print(json.dumps(line), flush=True)
@@ -658,13 +750,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
-                    choices=["uniform", "clustered", "small", "radial-pair", "infft", "learned", "batched"])
+                    choices=["uniform", "clustered", "small", "radial-pair", "infft", "learned", "batched",
+                             "convergence"])
     ap.add_argument("--plans", type=int, default=1024, help="plans of the batched workload")
     ap.add_argument("--train", type=int, default=256, help="training trajectories (learned)")
-    ap.add_argument("--test", type=int, default=8, help="held-out trajectories (learned)")
-    ap.add_argument("--epochs", type=int, default=3, help="training epochs (learned)")
+    ap.add_argument("--test", type=int, default=32, help="held-out trajectories (learned)")
+    ap.add_argument("--epochs", type=int, default=20, help="training epochs (learned)")
     ap.add_argument("--max-iter", type=int, default=3000, help="CGNR iteration cap (learned)")
     ap.add_argument("--iters", type=int, default=100, help="CGNR iterations of the iNFFT workload")
+    ap.add_argument("--solver", default="all", choices=["all", "fp64", "fp32", "fp32_refresh10"],
+                    help="solvers of the iNFFT workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the NDFT accuracy sample")
     args = ap.parse_args()
@@ -676,6 +771,8 @@ def main():
         return run_learned(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "convergence":
+        return run_convergence(args)
     wl =workload(args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)

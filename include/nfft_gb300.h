@@ -27,9 +27,11 @@ void *X(gb_get_stream)(X(plan) *ths); \
  * (no counterpart in the reference, whose double build needs none): the \
  * shared-memory subgrid keeps a second plane of rounding errors (error-free \
  * sums), the write-back adds them into the grid by error-free compare-and-swap \
- * with the remaining errors folded in before the FFT.  mode 1 on, 0 off, -1 \
- * the default (on for cut-off m >= 6).  Returns 0, or -1 (nothing changed) \
- * for a plan without such a kernel (double precision, d != 2, NDFT). */ \
+ * with the remaining errors folded in before the FFT.  It roughly doubles \
+ * the adjoint's B^T time and lowers the error only where very many nodes \
+ * share cells.  mode 1 on, 0 or -1 off (the default).  Returns 0, or -1 \
+ * (nothing changed) for a plan without such a kernel (double precision, \
+ * d != 2, NDFT). */ \
 int X(gb_set_compensated)(X(plan) *ths, int mode); \
 /* Device buffers of the plan: f_hat (N_total complex), f (M_total complex), \
  * in the caller's natural orders, and x (M_total*d reals, node-major). */ \

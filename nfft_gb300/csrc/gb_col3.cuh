@@ -21,8 +21,9 @@
 // tile's padded subgrid in shared memory as interleaved complex values.  A
 // warp takes a column chunk (at most 32 nodes of one column):
 //  * lane j evaluates node j's window into per-warp vectors: x scaled by f_j
-//    (complex; f_j read through the node permutation, the one scattered read
-//    of the adjoint), y, and z duplicated as (w, w) pairs;
+//    (complex), y, and z at its offset in an aligned pair; its node record
+//    and f_j (read through the node permutation, the one scattered read of
+//    the adjoint) were loaded while the warp's previous chunk computed;
 //  * lanes own (x, y) rows of the column (two per lane) and hold all
 //    8 + W - 1 z values of a row as complex accumulators in registers; for the
 //    nodes whose window starts at z0 (a compile-time case, eight of them)
@@ -205,28 +206,52 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   }
   const int ntask = __shfl_sync(0xffffffffu, incl, 15);
 
-  for (;;) {
-    int task = 0;
-    if (lane == 0) task = atomicAdd(taskctr, 1);
-    task = __shfl_sync(0xffffffffu, task, 0);
-    if (task >= ntask) break;
-    // column c = number of columns whose inclusive chunk count is <= task
-    const int c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
-    const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);  // lane c - 1 (c is warp-uniform)
+  // task -> (column, first node, node count)
+  auto locate = [&](int task, int &c, int &a, int &np) {
+    c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
+    const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);
     const int before = c > 0 ? prev : 0;
     const int clen = cstart[c + 1] - cstart[c];
     const int nchunk = (clen + C3_CHUNK - 1) / C3_CHUNK;
-    // the column's nodes split evenly into its chunks
     const int k = task - before, qn = clen / nchunk, rq = clen - qn * nchunk;
-    const int a = it.start + cstart[c] + k * qn + min(k, rq);
-    const int np = qn + (k < rq ? 1 : 0);
+    a = it.start + cstart[c] + k * qn + min(k, rq);
+    np = qn + (k < rq ? 1 : 0);
+  };
+  int task = 0;
+  if (lane == 0) task = atomicAdd(taskctr, 1);
+  task = __shfl_sync(0xffffffffu, task, 0);
+  int c = 0, a = 0, np = 0;
+  float4 rn = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 fn = make_float2(0.f, 0.f);
+  if (task < ntask) {
+    locate(task, c, a, np);
+    if (lane < np) {
+      rn = rec[a + lane];
+      fn = f[perm[a + lane]];
+    }
+  }
+  for (;;) {
+    if (task >= ntask) break;
     const int s0 = c >> 2, s1 = c & 3;
+    const float4 r = rn;
+    const float2 fj = fn;
+    const int np_cur = np;
+    // the next task's node data, loaded while this one computes
+    int ntaskid = 0;
+    if (lane == 0) ntaskid = atomicAdd(taskctr, 1);
+    ntaskid = __shfl_sync(0xffffffffu, ntaskid, 0);
+    int c2 = 0, a2 = 0, np2 = 0;
+    if (ntaskid < ntask) {
+      locate(ntaskid, c2, a2, np2);
+      if (lane < np2) {
+        rn = rec[a2 + lane];
+        fn = f[perm[a2 + lane]];
+      }
+    }
 
     // ---- set-up: lane j evaluates node j's window
     int z0 = 8;
-    if (lane < np) {
-      const float4 r = rec[a + lane];
-      const float2 fj = f[perm[a + lane]];
+    if (lane < np_cur) {
       const int loc = __float_as_int(r.w);
       float v[W];
       // x, scaled by f_j, at the node's offset in the column's box
@@ -294,7 +319,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
 #pragma unroll
     for (int z = 0; z <= 8; ++z) rs[z] = __popc(__ballot_sync(0xffffffffu, z0 < z));
     // z range the chunk touches: first z0 .. last z0 + W
-    const int zlo = __shfl_sync(0xffffffffu, z0, 0), zhi = __shfl_sync(0xffffffffu, z0, np - 1) + W;
+    const int zlo = __shfl_sync(0xffffffffu, z0, 0), zhi = __shfl_sync(0xffffffffu, z0, np_cur - 1) + W;
     __syncwarp();
 
 #pragma unroll 1
@@ -349,6 +374,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
                                                   ai[q], zlo, zhi);
     }
     __syncwarp();
+    task = ntaskid;
+    c = c2;
+    a = a2;
+    np = np2;
   }
   __syncthreads();
   // ---- write-back.  A tile whose padded box lies inside the grid: the box
@@ -401,10 +430,11 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
 // nfft_trafo_3d_compute, nfft.c:4020-4265).
 //
 // The nodes of a 2x2x2 sub-cell of a tile share one (W+1)^3 box of the padded
-// subgrid.  A CTA stages its tile's padded subgrid in shared memory as
-// interleaved complex rows of ZB cells (one TMA copy for a tile whose padded
-// box lies inside the grid, plain loads for one that wraps around the grid
-// edge), finds where each of the tile's 64 sub-cells starts in the
+// subgrid.  A CTA stages its tile's padded subgrid in shared memory as real
+// and imaginary planes (one TMA copy of the interleaved box, de-interleaved in
+// shared memory, for a tile whose padded box lies inside the grid; plain loads
+// for one that wraps around the grid edge), finds where each of the tile's 64
+// sub-cells starts in the
 // item's sorted node range, and its warps take units (at most S3_PM nodes of
 // one sub-cell, a sub-cell's nodes split evenly) from a shared counter:
 //  * lanes evaluate the unit's windows (one lane per node and dimension) into
@@ -425,27 +455,31 @@ struct S3 {
   static constexpr int RPL = 2;
   static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
   static constexpr int WARP_FLOATS = 3 * S3_PM * BOXP;  // wx, wy, wz [S3_PM][BOXP]
-  static constexpr int ZB = (EXT + 1) & ~1;              // cells of a subgrid row (16-byte rows)
-  // rows per x-plane of the staged subgrid: EXT rounded up to 3 mod 8, so that
-  // a plane is 3 bank groups of 16 bytes (mod 8) past the last but one and a
-  // row of ZB = 18 cells one: box rows (x, y) then fall in bank group
-  // (3x + y) mod 8, and any eight consecutive rows of the lanes' row order
-  // (y fastest, 11 per x) in eight different groups
+  static constexpr int INTS = 65 + 1;                   // sub-cell starts, task counter
+  // the TMA box of the padded subgrid: rows of ZB (even: 16-byte rows) complex
+  // cells, EXTY rows per x-plane -- EXT rounded up to 3 mod 8, so that the
+  // row-per-thread de-interleave reads consecutive rows from different banks
+  static constexpr int ZB = (EXT + 1) & ~1;
   static constexpr int EXTY = EXT + ((11 - EXT % 8) % 8);
-  static constexpr int GRID_CELLS = EXT * EXTY * ZB;     // the padded subgrid [EXT][EXTY][ZB]
-  static constexpr int INTS = 65 + 1;                    // sub-cell starts, task counter
   static_assert(BOXP > BOX, "the x vector needs one zero slot past the box");
-  static_assert(C3_WARPS * WARP_FLOATS * 4 % 128 == 0, "the subgrid starts on a 128-byte boundary");
 };
 
-// warp scratch | subgrid | ints | the TMA barrier (8-byte aligned)
+// warp scratch | real and imaginary planes | ints | (128-byte aligned) TMA
+// box | its barrier
 template <int W>
-__host__ __device__ inline size_t s3_smem_bytes(const Geom<float> &)
+__host__ __device__ inline size_t s3_box_offset(const Geom<float> &g)
 {
   typedef S3<W> P;
-  const size_t b = (size_t)C3_WARPS * P::WARP_FLOATS * sizeof(float) + (size_t)P::GRID_CELLS * sizeof(float2) +
-                   P::INTS * sizeof(int);
-  return (b + 7) / 8 * 8 + sizeof(unsigned long long);
+  const size_t b =
+      ((size_t)C3_WARPS * P::WARP_FLOATS + 2 * (size_t)P::EXT * g.sx) * sizeof(float) + P::INTS * sizeof(int);
+  return (b + 127) / 128 * 128;
+}
+
+template <int W>
+__host__ __device__ inline size_t s3_smem_bytes(const Geom<float> &g)
+{
+  typedef S3<W> P;
+  return s3_box_offset<W>(g) + (size_t)P::EXT * P::EXTY * P::ZB * sizeof(float2) + sizeof(unsigned long long);
 }
 
 template <int W>
@@ -459,18 +493,17 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
                                                             int use_tma)
 {
   typedef S3<W> P;
-  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RPL = P::RPL, PM = S3_PM, ZB = P::ZB;
+  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RPL = P::RPL, PM = S3_PM;
   extern __shared__ __align__(128) unsigned char c3_smem[];
   float *const base = reinterpret_cast<float *>(c3_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float *const wx = base + warp * P::WARP_FLOATS;
   float *const wy = wx + PM * BOXP;
   float *const wz = wy + PM * BOXP;
-  float2 *const sgrid = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
-  int *const sstart = reinterpret_cast<int *>(sgrid + P::GRID_CELLS);
+  float *const sre = base + C3_WARPS * P::WARP_FLOATS;
+  float *const sim = sre + EXT * g.sx;
+  int *const sstart = reinterpret_cast<int *>(sim + EXT * g.sx);
   int *const taskctr = sstart + 65;
-  unsigned long long *const bar = reinterpret_cast<unsigned long long *>(
-      c3_smem + (s3_smem_bytes<W>(g) - sizeof(unsigned long long)));
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
@@ -482,20 +515,26 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       rem /= g.ntile[t];
     }
   }
-  // the padded subgrid: one TMA copy where the box lies inside the grid
-  const bool tma = use_tma && org[0] + EXT <= g.n[0] && org[1] + EXT <= g.n[1] && org[2] + EXT <= g.n[2] &&
-                   (smem_u32(sgrid) & 127u) == 0;
   if (threadIdx.x == 0) {
-    if (tma) {
-      mbar_init(bar, 1);
-      mbar_expect_tx(bar, (unsigned)(P::GRID_CELLS * sizeof(float2)));
-      tma_load_3d(sgrid, &gmap, 2 * org[2], org[1], org[0], bar);
-    }
     c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
     c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
   }
+  // the padded subgrid: one TMA copy into the box where the box lies inside
+  // the grid (de-interleaved into the planes below), plain loads where it
+  // wraps around the grid edge
+  constexpr int ZB = P::ZB, EXTY = P::EXTY;
+  const size_t off = s3_box_offset<W>(g);
+  float2 *const stg = reinterpret_cast<float2 *>(c3_smem + off);
+  unsigned long long *const bar = reinterpret_cast<unsigned long long *>(c3_smem + off + (size_t)EXT * EXTY * ZB * sizeof(float2));
+  const bool tma = use_tma && org[0] + EXT <= g.n[0] && org[1] + EXT <= g.n[1] && org[2] + EXT <= g.n[2] &&
+                   (smem_u32(stg) & 127u) == 0;
+  if (threadIdx.x == 0 && tma) {
+    mbar_init(bar, 1);
+    mbar_expect_tx(bar, (unsigned)(EXT * EXTY * ZB * sizeof(float2)));
+    tma_load_3d(stg, &gmap, 2 * org[2], org[1], org[0], bar);
+  }
   if (!tma) {
-    // plain loads (the box wraps around the grid edge); several in flight per thread
+    // several grid loads in flight per thread
 #pragma unroll 4
     for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
       const int c2 = idx % EXT, r = idx / EXT;
@@ -504,7 +543,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
       while (p1 >= g.n[1]) p1 -= g.n[1];
       while (p2 >= g.n[2]) p2 -= g.n[2];
-      sgrid[(c0 * P::EXTY + c1) * ZB + c2] = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
+      const float2 v = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
+      const int si = c0 * g.sx + c1 * g.sy + c2;
+      sre[si] = v.x;
+      sim[si] = v.y;
     }
   }
   // the unused node slots of the weight vectors must hold finite values
@@ -520,6 +562,19 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
       if (threadIdx.x == 0) atomicAdd(&g_tma_wait_timeouts, 1ull);
       return;
     }
+    // de-interleave the box into the real and imaginary planes
+    for (int r = threadIdx.x; r < EXT * EXT; r += C3_THREADS) {
+      const int c0 = r / EXT, c1 = r - c0 * EXT;
+      const float2 *src = stg + (c0 * EXTY + c1) * ZB;
+      const int si = c0 * g.sx + c1 * g.sy;
+#pragma unroll
+      for (int z = 0; z < EXT; ++z) {
+        const float2 v = src[z];
+        sre[si + z] = v.x;
+        sim[si + z] = v.y;
+      }
+    }
+    __syncthreads();
   }
 
   // units per sub-cell: lane l holds sub-cells 2l and 2l+1
@@ -579,6 +634,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
     }
     __syncwarp();
 
+    const int sbase = b0 * g.sx + b1 * g.sy + b2;
     float acc[2 * PM];
 #pragma unroll
     for (int j = 0; j < 2 * PM; ++j) acc[j] = 0.f;
@@ -594,21 +650,22 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
         const int bx = rr / BOX;
         by[qq] = rr - bx * BOX;
         wbx[qq] = ok ? bx : BOXP - 1;  // rows past the box take the zero slot of the x vector
-        // rows of ZB (even) cells from an even sub-cell z origin start on a
-        // 16-byte boundary: two complex values per load
-        const float2 *pr = sgrid + ((b0 + bx) * P::EXTY + (b1 + by[qq])) * ZB + b2;
+        const float *pr = sre + sbase + bx * g.sx + by[qq] * g.sy;
+        const float *pi = sim + sbase + bx * g.sx + by[qq] * g.sy;
+        // row starts are even (even plane strides, even sub-cell z origin):
+        // pairs of z values load as 8-byte words
 #pragma unroll
         for (int z = 0; z + 1 < BOX; z += 2) {
-          const float4 a = *reinterpret_cast<const float4 *>(pr + z);
+          const float2 a = *reinterpret_cast<const float2 *>(pr + z);
+          const float2 b = *reinterpret_cast<const float2 *>(pi + z);
           gr[qq][z] = a.x;
-          gi[qq][z] = a.y;
-          gr[qq][z + 1] = a.z;
-          gi[qq][z + 1] = a.w;
+          gr[qq][z + 1] = a.y;
+          gi[qq][z] = b.x;
+          gi[qq][z + 1] = b.y;
         }
         if (BOX & 1) {
-          const float2 a = pr[BOX - 1];
-          gr[qq][BOX - 1] = a.x;
-          gi[qq][BOX - 1] = a.y;
+          gr[qq][BOX - 1] = pr[BOX - 1];
+          gi[qq][BOX - 1] = pi[BOX - 1];
         }
       }
 #pragma unroll

@@ -73,7 +73,7 @@ struct Ctx {
   WinPoly poly = {};     // polynomial window of the single-precision 2-D / 3-D kernels
   WinPolyD polyd = {};   // the same in double precision (2-D double-precision kernels)
   bool col2 = false;     // 2-D column kernels (nodes keyed by column)
-  int comp = -1;         // compensated 2-D single-precision B^T: 1 on, 0 off, -1 the default (on for m >= 6)
+  int comp = 0;          // compensated 2-D single-precision B^T (nfftf_gb_set_compensated), off by default
   void *grid_lo = nullptr;  // its error grid (n_total complex), allocated on first use
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
@@ -624,7 +624,7 @@ static bool bt2_stage(Ctx<R> *c, const typename Cx<R>::T *f)
   if (!c->col2) return false;
   if constexpr (std::is_same<R, float>::value) {
     float2 *lo = nullptr;
-    if (c->comp == 1 || (c->comp < 0 && c->g.m >= 6)) {
+    if (c->comp == 1) {
       if (!c->grid_lo) dev_alloc<R>(&c->grid_lo, (size_t)c->g.n_total * sizeof(float2));
       lo = (float2 *)c->grid_lo;
       GB_CUDA(cudaMemsetAsync(lo, 0, (size_t)c->g.n_total * sizeof(float2), c->stream));
@@ -948,14 +948,14 @@ static void init_default(typename Api<R>::plan *ths, int d, int *N, int M, int m
 }
 
 // ------------------------------------------------------------ extensions
-// mode 1 / 0 / -1 (default: on for m >= 6) for the compensated single-precision
-// 2-D column B^T; -1 returned where the plan runs no such kernel
+// mode 1 (on) / 0 (off, the default) / -1 (the default) for the compensated
+// single-precision 2-D column B^T; -1 returned where the plan runs no such kernel
 template <typename R>
 static int set_compensated(typename Api<R>::plan *ths, int mode)
 {
   Ctx<R> *c = ctx_of<R>(ths);
   if (!std::is_same<R, float>::value || c->g.d != 2 || c->direct || !c->col2 || mode < -1 || mode > 1) return -1;
-  c->comp = mode;
+  c->comp = mode == 1 ? 1 : 0;
   return 0;
 }
 

@@ -166,8 +166,3 @@ def build_training_set(lib, N, m, ids, arms=16, samples=8192, fp_iters=20):
         feats.append(raw_features(lib, x, n))
         targets.append(lw)
     return feats, targets
-
-
-def solve_to_tolerance(lib, N, x, m, y, f_ref, w, tol, single, max_iter):
-    return infft.time_to_tolerance(lib, single, N, x, m, y, f_ref, tol=tol, w=w,
-                                   refresh=10 if single else 0, max_iter=max_iter)

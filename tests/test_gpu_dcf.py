@@ -129,10 +129,8 @@ def test_learned_weights_speed_up_cgnr(gpulib):
     p.trafo()
     y = p.f.copy()
     p.finalize()
-    plain = infft.time_to_tolerance(gpulib, False, N, x, m, y, None, tol=1e-5, max_iter=4000,
-                                    criterion="residual")
-    learned = infft.time_to_tolerance(gpulib, False, N, x, m, y, None, tol=1e-5, w=w, max_iter=4000,
-                                      criterion="residual")
+    plain = infft.time_to_tolerance(gpulib, False, N, x, m, y, tol=1e-5, max_iter=4000)
+    learned = infft.time_to_tolerance(gpulib, False, N, x, m, y, tol=1e-5, w=w, max_iter=4000)
     plain.pop("f")
     learned.pop("f")
     print("plain", plain, "learned", learned, "loss", hist[0], hist[-1])

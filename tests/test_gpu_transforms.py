@@ -50,7 +50,11 @@ def ndft(N, x, fh, f, m=8):
 
 
 # ---------------------------------------------------------------- golden files
-INITS = ["dim", "default", "guru_pre_psi", "guru_pre_full_psi"]
+# tests/nfft.c:691-701 (its PRE_LIN_PSI variant is defined there and left out
+# of the run lists at 812; its PRE_FG_PSI one exists only for the Gaussian
+# window build).  This library evaluates the Kaiser-Bessel window exactly for
+# every PRE_*PSI flag, so each variant is held to the window's bound.
+INITS = ["dim", "default", "guru_pre_psi", "guru_pre_full_psi", "guru_pre_lin_psi", "guru_pre_fg_psi"]
 
 
 @pytest.mark.parametrize("single", [False, True])
@@ -73,6 +77,10 @@ def test_golden_files(gpulib, testdata, single, init):
             flags = default_guru_flags()
             if init == "guru_pre_full_psi":
                 flags = (flags & ~abi.PRE_PSI) | abi.PRE_FULL_PSI
+            elif init == "guru_pre_lin_psi":
+                flags = (flags & ~abi.PRE_PSI) | abi.PRE_LIN_PSI
+            elif init == "guru_pre_fg_psi":
+                flags = (flags & ~abi.PRE_PSI) | abi.FG_PSI | abi.PRE_FG_PSI
             p = make_plan(gpulib, single, N, M, flags=flags)
         p.x[:] = x
         if p.check() is not None:

@@ -516,7 +516,9 @@ def run_convergence(args):
     image error against the phantom and the image error in the band
     |nu| <= 0.45 the samples determine; reported: the steps to a 1e-5 residual
     and the smallest errors reached within --iters steps (unweighted; half as
-    many with weights)."""
+    many with weights).  A third setting runs the FP64 solver with the damping
+    of the reference's MRI reconstruction (PRECOMPUTE_DAMP, w_hat = 1 on the
+    image's inscribed disk, applications/mri/mri2d/reconstruct_data_2d.c)."""
     import torch
     import nfft_gb300
     from nfft_gb300 import dcf, infft, workloads
@@ -536,9 +538,14 @@ def run_convergence(args):
     res = infft.TrueResidual(lib, N, x, m, y)
     wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
     out = {}
-    for wname, w, total in (("unweighted", None, args.iters), ("fixed_point_weights", wfp, args.iters // 2)):
+    damp = infft.disk_damping(256)
+    settings = (("unweighted", None, None, args.iters), ("fixed_point_weights", wfp, None, args.iters // 2),
+                ("disk_damped", None, damp, args.iters))
+    for wname, w, wh, total in settings:
         for sname, single, refresh in (("fp64", False, 0), ("fp32", True, 0), ("fp32_refresh10", True, 10)):
-            s = infft.CGNR(lib, single, N, x, m, y, w=w, refresh=refresh)
+            if wh is not None and sname != "fp64":
+                continue
+            s = infft.CGNR(lib, single, N, x, m, y, w=w, refresh=refresh, w_hat=wh)
             s.set_sync(0)
             s.before_loop()
             rows = []

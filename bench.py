@@ -518,7 +518,8 @@ def run_convergence(args):
     and the smallest errors reached within --iters steps (unweighted; half as
     many with weights).  A third setting runs the FP64 solver with the damping
     of the reference's MRI reconstruction (PRECOMPUTE_DAMP, w_hat = 1 on the
-    image's inscribed disk, applications/mri/mri2d/reconstruct_data_2d.c)."""
+    image's inscribed disk, applications/mri/mri2d/reconstruct_data_2d.c) on
+    the phantom restricted to that disk."""
     import torch
     import nfft_gb300
     from nfft_gb300 import dcf, infft, workloads
@@ -538,14 +539,25 @@ def run_convergence(args):
     res = infft.TrueResidual(lib, N, x, m, y)
     wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
     out = {}
+    # the damped setting solves for the phantom restricted to the image's
+    # inscribed disk, from the data of that restricted phantom
     damp = infft.disk_damping(256)
+    q = Plan(lib, False, N, len(x), n=[512, 512], m=m, flags=infft.PLAN_FLAGS)
+    q.x[:] = x
+    q.precompute_one_psi()
+    q.f_hat[:] = f_true * damp
+    q.trafo()
+    y_disk = q.f.copy()
+    q.finalize()
+    res_disk = infft.TrueResidual(lib, N, x, m, y_disk)
     settings = (("unweighted", None, None, args.iters), ("fixed_point_weights", wfp, None, args.iters // 2),
                 ("disk_damped", None, damp, args.iters))
     for wname, w, wh, total in settings:
+        yy, ft, rr = (y_disk, f_true * damp, res_disk) if wh is not None else (y, f_true, res)
         for sname, single, refresh in (("fp64", False, 0), ("fp32", True, 0), ("fp32_refresh10", True, 10)):
             if wh is not None and sname != "fp64":
                 continue
-            s = infft.CGNR(lib, single, N, x, m, y, w=w, refresh=refresh, w_hat=wh)
+            s = infft.CGNR(lib, single, N, x, m, yy, w=w, refresh=refresh, w_hat=wh)
             s.set_sync(0)
             s.before_loop()
             rows = []
@@ -553,7 +565,7 @@ def run_convergence(args):
                 s.steps(10)
                 s.sync()
                 f = s.f_hat
-                rows.append(((k + 1) * 10, res(f)) + infft.image_errors(f, f_true))
+                rows.append(((k + 1) * 10, rr(f)) + infft.image_errors(f, ft))
             s.close()
             a = np.array(rows)
             out["%s/%s" % (wname, sname)] = {
@@ -561,6 +573,7 @@ def run_convergence(args):
                 "min_resid": float(a[:, 1].min()), "min_image_err": float(a[:, 2].min()),
                 "min_band_err": float(a[:, 3].min()), "steps": total}
     res.close()
+    res_disk.close()
     line = {"metric": "CGNR convergence on one spiral trajectory (2-D, N=256^2, m=6, noiseless)",
             "value": out["unweighted/fp32"]["steps_to_resid_1e-5"], "unit": "steps", "n_gpus": 1,
             "higher_is_better": False, "data": "synthetic", "runs": out}

@@ -57,3 +57,44 @@ def test_sort_of_2e24_nodes_is_bit_exact(gpulib, dist):
     o.close()
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, "first difference at %d of %d" % (bad[0], got.size)
+
+
+@pytest.mark.parametrize("dist", ["uniform", "clustered"])
+def test_full_3d_size_adjointness_and_linearity(gpulib, dist):
+    """At the full 3-D single-precision size (N = 128^3, n = 256^3, m = 4,
+    M = 2^24), properties that hold at any size: the adjoint is the adjoint,
+    <A fh, f> = <fh, A^H f> (relative to |A fh| |f|), and the transform is
+    linear, A(a u + b v) = a A u + b A v -- both to single-precision accuracy."""
+    N, n, m, M = [128] * 3, [256] * 3, 4, 1 << 24
+    NN = 128 ** 3
+    x = workloads.cube_nodes(M, 3, dist, 0)
+    flags = (abi.PRE_PHI_HUT | abi.PRE_PSI | abi.MALLOC_X | abi.MALLOC_F_HAT | abi.MALLOC_F
+             | abi.FFTW_INIT | abi.FFT_OUT_OF_PLACE | abi.NFFT_SORT_NODES)
+    p = Plan(gpulib, True, N, M, n=n, m=m, flags=flags)
+    p.x[:] = x
+    p.precompute_one_psi()
+    rng = np.random.default_rng(4)
+    u = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    v = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
+    a, b = np.complex64(0.75 - 0.5j), np.complex64(-1.25 + 0.25j)
+    p.f_hat[:] = u
+    p.trafo()
+    Au = p.f.astype(np.complex128)
+    p.f_hat[:] = v
+    p.trafo()
+    Av = p.f.astype(np.complex128)
+    p.f_hat[:] = a * u + b * v
+    p.trafo()
+    Aw = p.f.astype(np.complex128)
+    p.f[:] = f
+    p.adjoint()
+    AHf = p.f_hat.astype(np.complex128)
+    p.finalize()
+    lhs = np.vdot(f.astype(np.complex128), Au)   # <A u, f> = f^H A u
+    rhs = np.vdot(AHf, u.astype(np.complex128))  # <u, A^H f> = (A^H f)^H u
+    adj = abs(lhs - rhs) / (np.linalg.norm(Au) * np.linalg.norm(f))
+    lin = np.linalg.norm(Aw - (complex(a) * Au + complex(b) * Av)) / np.linalg.norm(Aw)
+    print("%s 2^24 nodes: adjointness %.2e, linearity %.2e" % (dist, adj, lin))
+    assert adj < 1e-5, adj
+    assert lin < 1e-5, lin

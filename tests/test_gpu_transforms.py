@@ -362,3 +362,27 @@ def test_repeated_calls_and_no_precompute_flags(gpulib):
     tf, _ = ndft(N, x2, fh, f)
     assert rel_l2(b, tf) < 1e-9
     assert rel_l2(b, np.roll(a, 7)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [[36, 40, 34], [40, 36, 33], [16, 16, 16], [24, 16, 40]])
+def test_3d_single_grids_with_and_without_tma_tiles(gpulib, n):
+    """The 3-D single-precision kernels on grids where the TMA paths do not all
+    apply: an odd last grid length (no tensor map: every tile staged and
+    written back cell by cell), grids smaller than the padded tile (every tile
+    wraps around the grid edge) and mixes of interior and edge tiles.  Both
+    transforms against the oracle; no bounded TMA wait may have given up."""
+    import ctypes as C
+    N, M, m = [16, 16, 16], 6000, 4
+    x, fh, f = seeded_case(N, M, seed=31)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    got_f, got_fh = run_both(p, x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64))
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m)
+    o.set_nodes(x.astype(np.float32).astype(np.float64))
+    o.precompute()
+    e_t = rel_l2(got_f.astype(np.complex128), o.trafo(fh.astype(np.complex64).astype(np.complex128)))
+    e_a = rel_l2(got_fh.astype(np.complex128), o.adjoint(f.astype(np.complex64).astype(np.complex128)))
+    assert e_t < 1e-5 and e_a < 1e-5, (n, e_t, e_a)
+    fn = gpulib.nfft_gb_tma_wait_timeouts
+    fn.restype = C.c_ulonglong
+    assert fn() == 0

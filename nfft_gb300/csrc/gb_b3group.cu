@@ -9,9 +9,9 @@
 
 namespace gb {
 
-int col3_b_ext_y(int w)
+int col3_box_ext_y(int w)
 {
-  return w == 10 ? S3<10>::EXTY : 8 + w - 1;
+  return w == 10 ? Box3<10>::EXTY : 8 + w - 1;
 }
 
 unsigned long long read_wait_timeouts()
@@ -34,12 +34,12 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
     // the grid's TMA view (a zeroed map and use_tma = 0 where there is none)
     CUtensorMap gmap;
     memset(&gmap, 0, sizeof(gmap));
-    const int use_tma = cb.grid_map && cb.grid_map_b ? 1 : 0;
-    if (use_tma) gmap = adjoint ? *cb.grid_map : *cb.grid_map_b;
+    const int use_tma = cb.grid_map ? 1 : 0;
+    if (use_tma) gmap = *cb.grid_map;
     if (adjoint) {
-      set_smem_limit((const void *)k_bt3_col<W>, c3_smem_bytes<W>(g));
-      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly,
-                                                                   gmap, use_tma);
+      set_smem_limit((const void *)k_bt3_col<W>, c3_smem_bytes<W>());
+      k_bt3_col<W><<<nitems, C3_THREADS, c3_smem_bytes<W>(), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly,
+                                                                  gmap, use_tma);
       GB_LAUNCHED("bt3_col");
       return;
     }
@@ -68,7 +68,7 @@ template <> struct G3Set<float> {
   {
     switch (g.w) {
       case 8: return g3_smem_max<float, 8, G3_CS>(g);
-      case 10: return std::max({g3_smem_max<float, 10, G3_CS>(g), c3_smem_bytes<10>(g), s3_smem_bytes<10>(g)});
+      case 10: return std::max({g3_smem_max<float, 10, G3_CS>(g), c3_smem_bytes<10>(), s3_smem_bytes<10>(g)});
       case 14: return g3_smem_max<float, 14, G3_CS>(g);
     }
     return 0;

@@ -1,11 +1,18 @@
-// gb_col3.cuh -- single-precision 3-D B^T (adjoint spreading) by z-columns
-// and 3-D B (interpolation) by sub-cell units: the hot kernels of the 3-D
-// transform.
+// gb_col3.cuh -- single-precision 3-D B^T (adjoint spreading) by z-column
+// segments and 3-D B (interpolation) by sub-cell units: the hot kernels of the
+// 3-D transform.
 //
 // Both evaluate the Kaiser-Bessel window on the fly from its per-tap
 // polynomial form (gb_window.cpp): degree-9 Horner in the node's fractional
 // grid offset, single-precision FMAs with the coefficients as kernel
-// parameters.
+// parameters, taps l and W-1-l from one even/odd split.
+//
+// Both keep a tile's padded subgrid in shared memory in the layout of one TMA
+// box of the grid: EXT x-planes of EXTY rows of ZB interleaved complex cells
+// (EXT = 8 + W - 1 cells used per dimension; ZB = EXT rounded up to even, so
+// that rows are 16-byte multiples; EXTY = EXT rounded up to 3 mod 8, so that
+// consecutive rows of a plane fall in different banks).  The cells past EXT
+// stay zero.
 //
 // B^T -- reference nfft_adjoint_3d_B (nfft.c:5126-5384) with its blockwise
 // scatter (nfft.c:4289-4388): g[l mod n] += phi_0 phi_1 phi_2 f_j over the
@@ -17,28 +24,32 @@
 // the same W+1 by W+1 (x, y) rows of the tile's padded subgrid, over z in
 // [0, 8 + W - 1).
 //
-// A CTA takes one work item (a tile and a range of its nodes) and keeps the
-// tile's padded subgrid in shared memory as interleaved complex values.  A
-// warp takes a column chunk (at most 32 nodes of one column):
-//  * lane j evaluates node j's window into per-warp vectors: x scaled by f_j
-//    (complex), y, and z at its offset in an aligned pair; its node record
-//    and f_j (read through the node permutation, the one scattered read of
-//    the adjoint) were loaded while the warp's previous chunk computed;
-//  * lanes own (x, y) rows of the column (two per lane) and hold all
-//    8 + W - 1 z values of a row as complex accumulators in registers; for the
-//    nodes whose window starts at z0 (a compile-time case, eight of them)
-//    each row takes exactly W paired FMAs (fma.rn.f32x2 of the sm_100
-//    family: real and imaginary at once);
-//  * each row is added to the shared subgrid once per chunk.  Single-precision
-//    atomic adds on shared memory are compare-and-swap loops, one value at a
-//    time; here a row's complex cells are read, summed and swapped as 64-bit
-//    words, all of them before the first result is checked, and only the
-//    rare cell another warp changed in between is added again;
-//  * the subgrid goes to the global grid once per work item: a tile whose
-//    padded box lies inside the grid is copied into a dense box in the
-//    warps' (then idle) scratch and added to the grid by one TMA add-reduce
-//    (cp.reduce.async.bulk.tensor); a tile whose box wraps around the grid
-//    edge adds its cells with vector reductions.
+// A CTA takes one work item (a tile and a range of its nodes) and zeroes the
+// tile's padded subgrid.  Its warps work in pairs; a pair takes column
+// segments (at most C3_SEGN nodes of one column, a long column's nodes split
+// evenly) from a shared counter:
+//  * the lanes of a pair own the column's rows, two per lane in each warp
+//    (row = lane + 32 (2 h + q) for warp h of the pair), and hold all
+//    8 + W - 1 z values of a row as real and imaginary accumulator pairs in
+//    registers for the whole segment;
+//  * the segment goes in chunks of 32 nodes: lane j of one warp evaluates
+//    node j's x window scaled by f_j (complex), lane j of the other its y
+//    window and its z window at the parity of its start, into the pair's
+//    node records in shared memory; the next chunk's node records and f_j
+//    (read through the node permutation, the one scattered read of the
+//    adjoint) are loaded while the current chunk computes;
+//  * for the nodes whose window starts at z0 (a compile-time case, eight of
+//    them) each row takes exactly W or W + 2 paired FMAs (fma.rn.f32x2 of the
+//    sm_100 family: two z values at once);
+//  * at the end of a segment each row is added to the shared subgrid two
+//    cells at a time: a 16-byte read, two paired adds and a 128-bit
+//    compare-and-swap (atom.shared.cas.b128), all of a block's cells read
+//    before the first swap; a cell pair another warp changed in between is
+//    added again with per-component atomic adds;
+//  * the subgrid goes to the global grid once per work item: a tile whose box
+//    lies inside the grid by one TMA add-reduce (cp.reduce.async.bulk.tensor)
+//    straight from the subgrid; a tile whose box wraps around the grid edge
+//    adds its cells with vector reductions.
 #pragma once
 
 #include "gb_b3group.cuh"  // warp_transpose_reduce
@@ -53,50 +64,49 @@ __device__ unsigned long long g_tma_wait_timeouts;
 
 static constexpr int C3_THREADS = 256;
 static constexpr int C3_WARPS = C3_THREADS / 32;
-static constexpr int C3_CHUNK = 32;  // nodes per column chunk (one per lane at set-up)
+static constexpr int C3_PAIRS = C3_WARPS / 2;
+static constexpr int C3_CHUNK = 32;    // nodes per chunk (one per lane at set-up)
+static constexpr int C3_SEGN = 256;    // nodes per column segment at most
 
+// the padded subgrid of a tile, as the TMA box of the grid
 template <int W>
-struct C3 {
-  static constexpr int EXT = 8 + W - 1;                      // padded subgrid edge
-  static constexpr int BOX = W + 1;                          // rows per dimension of a column
-  static constexpr int BOXP = (BOX + 3) / 4 * 4;             // padded x / y vector length
-  static constexpr int ROWS = BOX * BOX;                     // (x, y) rows of a column
-  static constexpr int RPL = 2;                              // rows a lane holds at once
-  static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
-  static constexpr int ZP = (W + 2 + 3) / 4 * 4;            // z taps with a parity shift, padded
-  static constexpr int NPAIR = (EXT + 1) / 2;                // z pairs of a row's accumulators
-  // per-warp scratch (floats): x scaled by f [CHUNK][BOXP] complex, y
-  // [CHUNK][BOXP], z [CHUNK][ZP] shifted by the parity of the window start
-  static constexpr int WXF = 0;
-  static constexpr int WY = WXF + 2 * BOXP * C3_CHUNK;
-  static constexpr int WZ = WY + BOXP * C3_CHUNK;
-  static constexpr int WARP_FLOATS = WZ + ZP * C3_CHUNK;
-  static constexpr int INTS = 17 + 1;                        // column starts, task counter
-  static_assert(BOXP > BOX, "x / y vectors need one zero slot past the column");
-  static_assert(W % 2 == 0, "even window width");
+struct Box3 {
+  static constexpr int EXT = 8 + W - 1;
+  static constexpr int ZB = (EXT + 1) & ~1;
+  static constexpr int EXTY = EXT + ((11 - EXT % 8) % 8);
+  static constexpr int SY = ZB, SX = EXTY * ZB;  // row and plane strides (complex cells)
+  static constexpr size_t BYTES = (size_t)EXT * SX * sizeof(float2);
 };
 
 template <int W>
-inline size_t c3_smem_bytes(const Geom<float> &g)
+struct C3 {
+  static constexpr int EXT = Box3<W>::EXT;
+  static constexpr int BOX = W + 1;                 // rows per dimension of a column
+  static constexpr int BOXP = (BOX + 3) / 4 * 4;    // padded x / y vector length
+  static constexpr int ROWS = BOX * BOX;            // (x, y) rows of a column
+  static constexpr int RQ = 2;                      // rows per lane in each warp of a pair
+  static constexpr int ZP = (W + 2 + 3) / 4 * 4;   // z taps with a parity shift, padded
+  static constexpr int NPAIR = Box3<W>::ZB / 2;     // z pairs of a row
+  // per-node record (floats): x scaled by f [BOXP] complex | y [BOXP] | z
+  // [ZP] at the parity of the window start
+  static constexpr int NXF = 0, NY = 2 * BOXP, NZ = 3 * BOXP, NF = 3 * BOXP + ZP;
+  static constexpr size_t SUBGRID = (Box3<W>::BYTES + 127) / 128 * 128;
+  static_assert(BOXP > BOX, "x / y vectors need one zero slot past the column");
+  static_assert(W % 2 == 0, "even window width");
+  static_assert(ROWS <= 4 * 32, "a pair's lanes hold the column's rows");
+  static_assert(NPAIR * 2 >= EXT, "z pairs cover the padded tile");
+};
+
+template <int W>
+inline size_t c3_smem_bytes()
 {
   typedef C3<W> P;
-  return (size_t)C3_WARPS * P::WARP_FLOATS * sizeof(float) + (size_t)P::EXT * g.sx2 * sizeof(float2)
-         + P::INTS * sizeof(int);
-}
-
-__device__ __forceinline__ unsigned long long f2_bits(float2 v)
-{
-  union {
-    float2 f;
-    unsigned long long u;
-  } c;
-  c.f = v;
-  return c.u;
+  return P::SUBGRID + (size_t)C3_PAIRS * P::NF * C3_CHUNK * sizeof(float) + (17 + 1 + C3_PAIRS) * sizeof(int);
 }
 
 // Starts a bulk copy of the 16-byte aligned interior of [p, p + bytes) from
 // global memory into L2 (cp.async.bulk.prefetch, sm_90 and later): the
-// work item's node data arrive while the CTA stages its subgrid.
+// work item's node data arrive while the CTA zeroes or stages its subgrid.
 __device__ __forceinline__ void c3_prefetch_l2(const void *p, long long bytes)
 {
   const unsigned long long a = (unsigned long long)p;
@@ -107,49 +117,41 @@ __device__ __forceinline__ void c3_prefetch_l2(const void *p, long long bytes)
   }
 }
 
-// Adds v[z] to the interleaved complex cells p[z], z < N, ZB cells at a time
-// (blocks wholly outside the warp-uniform range [z1, z2) hold zeros and are
-// skipped):
-// every cell of a block is read, summed (one paired add) and offered by one
-// 64-bit compare-and-swap before any result is checked; a cell whose swap
-// found a value changed by another warp in between is added again with the
-// atomic add of each component.
-template <int N, int NP, int ZB>
-__device__ __forceinline__ void c3_flush_row(float2 *p, const float2 (&vr)[NP], const float2 (&vi)[NP], int z1,
-                                             int z2)
+// 16-byte shared-memory read that sees other warps' stores
+__device__ __forceinline__ float4 lds_v4_volatile(unsigned a)
 {
-  static_assert(N <= 2 * NP, "cells past the accumulators");
-  volatile float2 *vp = p;
-#pragma unroll
-  for (int z0 = 0; z0 < N; z0 += ZB) {
-    if (z0 + ZB <= z1 || z0 >= z2) continue;
-    float2 cur[ZB], v[ZB];
-#pragma unroll
-    for (int e = 0; e < ZB; ++e)
-      if (z0 + e < N) {
-        const int z = z0 + e;
-        const volatile float2 &c = vp[z];
-        cur[e] = make_float2(c.x, c.y);
-        v[e] = make_float2((z & 1) ? vr[z >> 1].y : vr[z >> 1].x, (z & 1) ? vi[z >> 1].y : vi[z >> 1].x);
-      }
-    unsigned miss = 0;
-#pragma unroll
-    for (int e = 0; e < ZB; ++e) {
-      if (z0 + e < N) {
-        const unsigned long long old = f2_bits(cur[e]);
-        const unsigned long long want = f2_bits(__fadd2_rn(cur[e], v[e]));
-        if (atomicCAS(reinterpret_cast<unsigned long long *>(p + z0 + e), old, want) != old) miss |= 1u << e;
-      }
-    }
-    if (miss) {
-#pragma unroll
-      for (int e = 0; e < ZB; ++e)
-        if (z0 + e < N && (miss >> e) & 1u) {
-          atomicAdd(&p[z0 + e].x, v[e].x);
-          atomicAdd(&p[z0 + e].y, v[e].y);
-        }
-    }
-  }
+  float4 v;
+  asm volatile("ld.volatile.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(a));
+  return v;
+}
+
+// 128-bit compare-and-swap on shared memory (sm_90 and later); true where it
+// swapped
+__device__ __forceinline__ bool cas128_shared(unsigned a, float4 expect, float4 want)
+{
+  const unsigned long long e0 = ((unsigned long long)__float_as_uint(expect.y) << 32) | __float_as_uint(expect.x);
+  const unsigned long long e1 = ((unsigned long long)__float_as_uint(expect.w) << 32) | __float_as_uint(expect.z);
+  const unsigned long long w0 = ((unsigned long long)__float_as_uint(want.y) << 32) | __float_as_uint(want.x);
+  const unsigned long long w1 = ((unsigned long long)__float_as_uint(want.w) << 32) | __float_as_uint(want.z);
+  unsigned long long o0, o1;
+  asm volatile(
+      "{\n\t.reg .b128 e, w, o;\n\t"
+      "mov.b128 e, {%2, %3};\n\t"
+      "mov.b128 w, {%4, %5};\n\t"
+      "atom.shared.cas.b128 o, [%6], e, w;\n\t"
+      "mov.b128 {%0, %1}, o;\n\t}"
+      : "=l"(o0), "=l"(o1)
+      : "l"(e0), "l"(e1), "l"(w0), "l"(w1), "r"(a)
+      : "memory");
+  return o0 == e0 && o1 == e1;
+}
+
+// the two warps of pair p (named barrier p + 1; barrier 0 is __syncthreads)
+__device__ __forceinline__ void pair_sync(int p)
+{
+  asm volatile("bar.sync %0, 64;" ::"r"(p + 1) : "memory");
 }
 
 template <int W>
@@ -163,17 +165,18 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
                                                             int use_tma)
 {
   typedef C3<W> P;
-  constexpr int EXT = P::EXT, BOXP = P::BOXP, RPL = P::RPL;
+  typedef Box3<W> B;
+  constexpr int EXT = P::EXT, BOX = P::BOX, BOXP = P::BOXP, RQ = P::RQ, NF = P::NF;
+  constexpr int SX = B::SX, SY = B::SY;
   extern __shared__ __align__(128) unsigned char c3_smem[];
-  float *const base = reinterpret_cast<float *>(c3_smem);
+  float2 *const sg = reinterpret_cast<float2 *>(c3_smem);
+  float *const scratch = reinterpret_cast<float *>(c3_smem + P::SUBGRID);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *const wsc = base + warp * P::WARP_FLOATS;
-  float2 *const wxf = reinterpret_cast<float2 *>(wsc + P::WXF);
-  float *const wy = wsc + P::WY;
-  float *const wz = wsc + P::WZ;
-  float2 *const sg = reinterpret_cast<float2 *>(base + C3_WARPS * P::WARP_FLOATS);
-  int *const cstart = reinterpret_cast<int *>(sg + EXT * g.sx2);
+  const int pair = warp >> 1, half = warp & 1;
+  float *const wsc = scratch + pair * NF * C3_CHUNK;
+  int *const cstart = reinterpret_cast<int *>(scratch + C3_PAIRS * NF * C3_CHUNK);
   int *const taskctr = cstart + 17;
+  int *const nextslot = taskctr + 1 + pair;  // the pair's next task, posted by its first warp
 
   const WorkItem it = items[blockIdx.x];
   int org[3];
@@ -189,174 +192,186 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
     c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
     c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
   }
-  for (int i = threadIdx.x; i < EXT * g.sx2; i += C3_THREADS) sg[i] = make_float2(0.f, 0.f);
+  {
+    float4 *z4 = reinterpret_cast<float4 *>(sg);
+    for (int i = threadIdx.x; i < EXT * SX / 2; i += C3_THREADS) z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   // column boundaries of the item (node set-up): cstart[c] = first node of column c
   if (threadIdx.x < 17) cstart[threadIdx.x] = cst[17LL * blockIdx.x + threadIdx.x];
   if (threadIdx.x == 0) *taskctr = 0;
   __syncthreads();
 
-  // chunks per column (lanes 0..15), inclusive scan -> task -> column map
-  int nch = 0;
-  if (lane < 16) nch = (cstart[lane + 1] - cstart[lane] + C3_CHUNK - 1) / C3_CHUNK;
-  int incl = nch;
+  // segments per column (lanes 0..15), inclusive scan -> task -> column map
+  int nseg = 0;
+  if (lane < 16) nseg = (cstart[lane + 1] - cstart[lane] + C3_SEGN - 1) / C3_SEGN;
+  int incl = nseg;
 #pragma unroll
   for (int o = 1; o < 16; o <<= 1) {
     const int v = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += v;
   }
   const int ntask = __shfl_sync(0xffffffffu, incl, 15);
-
   // task -> (column, first node, node count)
   auto locate = [&](int task, int &c, int &a, int &np) {
     c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
     const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);
     const int before = c > 0 ? prev : 0;
     const int clen = cstart[c + 1] - cstart[c];
-    const int nchunk = (clen + C3_CHUNK - 1) / C3_CHUNK;
-    const int k = task - before, qn = clen / nchunk, rq = clen - qn * nchunk;
+    const int ns = (clen + C3_SEGN - 1) / C3_SEGN;
+    const int k = task - before, qn = clen / ns, rq = clen - qn * ns;
     a = it.start + cstart[c] + k * qn + min(k, rq);
     np = qn + (k < rq ? 1 : 0);
   };
-  int task = 0;
-  if (lane == 0) task = atomicAdd(taskctr, 1);
-  task = __shfl_sync(0xffffffffu, task, 0);
+
+  // byte offsets of the lane's rows' x and y weights in a node record (rows
+  // past the column read the zero slot BOXP - 1 of the x vector)
+  int xo[RQ], yo[RQ];
+#pragma unroll
+  for (int q = 0; q < RQ; ++q) {
+    const int row = lane + 32 * (2 * half + q);
+    const bool ok = row < P::ROWS;
+    const int bx = ok ? row / BOX : 0, by = ok ? row - (row / BOX) * BOX : 0;
+    xo[q] = 4 * P::NXF + 8 * (ok ? bx : BOXP - 1);
+    yo[q] = 4 * P::NY + 4 * by;
+  }
+
+  // the pair's first task: its first warp takes it, both read it
+  if (half == 0 && lane == 0) *nextslot = atomicAdd(taskctr, 1);
+  pair_sync(pair);
+  int task = *nextslot;
+  pair_sync(pair);
   int c = 0, a = 0, np = 0;
   float4 rn = make_float4(0.f, 0.f, 0.f, 0.f);
   float2 fn = make_float2(0.f, 0.f);
   if (task < ntask) {
     locate(task, c, a, np);
-    if (lane < np) {
+    if (lane < min(np, C3_CHUNK)) {
       rn = rec[a + lane];
-      fn = f[perm[a + lane]];
+      if (half == 0) fn = f[perm[a + lane]];
     }
   }
-  for (;;) {
-    if (task >= ntask) break;
+  while (task < ntask) {
     const int s0 = c >> 2, s1 = c & 3;
-    const float4 r = rn;
-    const float2 fj = fn;
-    const int np_cur = np;
-    // the next task's node data, loaded while this one computes
-    int ntaskid = 0;
-    if (lane == 0) ntaskid = atomicAdd(taskctr, 1);
-    ntaskid = __shfl_sync(0xffffffffu, ntaskid, 0);
-    int c2 = 0, a2 = 0, np2 = 0;
-    if (ntaskid < ntask) {
-      locate(ntaskid, c2, a2, np2);
-      if (lane < np2) {
-        rn = rec[a2 + lane];
-        fn = f[perm[a2 + lane]];
-      }
-    }
-
-    // ---- set-up: lane j evaluates node j's window
-    int z0 = 8;
-    if (lane < np_cur) {
+    // real and imaginary accumulators of the rows' z values, as aligned pairs
+    float2 ar[RQ][P::NPAIR], ai[RQ][P::NPAIR];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q)
+#pragma unroll
+      for (int z = 0; z < P::NPAIR; ++z) ar[q][z] = ai[q][z] = make_float2(0.f, 0.f);
+    int zlo = 8, zhi = 0;  // z range the segment touches
+    int off = 0;
+    int ntaskid = task, c2 = c, a2 = a, np2 = np;
+    for (;;) {
+      const float4 r = rn;
+      const float2 fj = fn;
+      const int npc = min(C3_CHUNK, np - off);
+      int off2 = off + C3_CHUNK;
+      const bool last = off2 >= np;  // the segment's last chunk: the next is the next task's first
+      if (last && half == 0 && lane == 0) *nextslot = atomicAdd(taskctr, 1);
+      // ---- set-up: lane j evaluates node j's windows, x (scaled by f_j) in
+      // the pair's first warp, y and z in its second
       const int loc = __float_as_int(r.w);
-      float v[W];
-      // x, scaled by f_j, at the node's offset in the column's box
-      const int ox = (loc & 7) - 2 * s0;
-      kb_poly_taps_sym<W>(r.x, poly.c[0], v);
-      {
-        float4 *dst = reinterpret_cast<float4 *>(wxf + lane * BOXP);
+      int z0 = 8;
+      if (lane < npc) {
+        float *nd = wsc + lane * NF;
+        float v[W];
+        z0 = loc >> 6;
+        if (half == 0) {
+          const int ox = (loc & 7) - 2 * s0;  // the node's x offset in the column's box
+          kb_poly_taps_sym<W>(r.x, poly.c[0], v);
+          float4 *dst = reinterpret_cast<float4 *>(nd + P::NXF);
 #pragma unroll
-        for (int q = 0; q < BOXP / 2; ++q) {
-          float e[4];
+          for (int q = 0; q < BOXP / 2; ++q) {
+            float e[4];
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int b = 2 * q + h;
-            float val = 0.f;
-            if (b < W && ox == 0) val = v[b];
-            if (b >= 1 && b - 1 < W && ox == 1) val = v[b - 1];
-            e[2 * h] = val * fj.x;
-            e[2 * h + 1] = val * fj.y;
+            for (int h = 0; h < 2; ++h) {
+              const int b = 2 * q + h;
+              float val = 0.f;
+              if (b < W && ox == 0) val = v[b];
+              if (b >= 1 && b - 1 < W && ox == 1) val = v[b - 1];
+              e[2 * h] = val * fj.x;
+              e[2 * h + 1] = val * fj.y;
+            }
+            dst[q] = make_float4(e[0], e[1], e[2], e[3]);
           }
-          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+        } else {
+          const int oy = ((loc >> 3) & 7) - 2 * s1;
+          kb_poly_taps_sym<W>(r.y, poly.c[1], v);
+          {
+            float4 *dst = reinterpret_cast<float4 *>(nd + P::NY);
+#pragma unroll
+            for (int q = 0; q < BOXP / 4; ++q) {
+              float e[4];
+#pragma unroll
+              for (int h = 0; h < 4; ++h) {
+                const int b = 4 * q + h;
+                float val = 0.f;
+                if (b < W && oy == 0) val = v[b];
+                if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
+                e[h] = val;
+              }
+              dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+            }
+          }
+          // taps at the node's z offset within its aligned pair: a window
+          // starting at odd z0 begins in the second half of a pair
+          kb_poly_taps_sym<W>(r.z, poly.c[2], v);
+          const int oz = z0 & 1;
+          float4 *dst = reinterpret_cast<float4 *>(nd + P::NZ);
+#pragma unroll
+          for (int q = 0; q < P::ZP / 4; ++q) {
+            float e[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              const int b = 4 * q + h;
+              float val = 0.f;
+              if (b < W && oz == 0) val = v[b];
+              if (b >= 1 && b - 1 < W && oz == 1) val = v[b - 1];
+              e[h] = val;
+            }
+            dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+          }
         }
       }
-      const int oy = ((loc >> 3) & 7) - 2 * s1;
-      kb_poly_taps_sym<W>(r.y, poly.c[1], v);
-      {
-        float4 *dst = reinterpret_cast<float4 *>(wy + lane * BOXP);
-#pragma unroll
-        for (int q = 0; q < BOXP / 4; ++q) {
-          float e[4];
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int b = 4 * q + h;
-            float val = 0.f;
-            if (b < W && oy == 0) val = v[b];
-            if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
-            e[h] = val;
-          }
-          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+      zlo = min(zlo, __shfl_sync(0xffffffffu, z0, 0));
+      zhi = max(zhi, __shfl_sync(0xffffffffu, z0, npc - 1) + W);
+      pair_sync(pair);  // the chunk's node records are written; the next task id is posted
+      // the next chunk's node data, loaded while this one computes
+      if (last) {
+        off2 = 0;
+        ntaskid = *nextslot;
+        if (ntaskid < ntask) locate(ntaskid, c2, a2, np2);
+      }
+      if (ntaskid < ntask) {
+        const int n2 = min(C3_CHUNK, np2 - off2);
+        if (lane < n2) {
+          rn = rec[a2 + off2 + lane];
+          if (half == 0) fn = f[perm[a2 + off2 + lane]];
         }
       }
-      z0 = loc >> 6;
-      kb_poly_taps_sym<W>(r.z, poly.c[2], v);
-      {
-        // taps at the node's z offset within its aligned pair: a window
-        // starting at odd z0 begins in the second half of a pair
-        const int oz = z0 & 1;
-        float4 *dst = reinterpret_cast<float4 *>(wz + lane * P::ZP);
-#pragma unroll
-        for (int q = 0; q < P::ZP / 4; ++q) {
-          float e[4];
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int b = 4 * q + h;
-            float val = 0.f;
-            if (b < W && oz == 0) val = v[b];
-            if (b >= 1 && b - 1 < W && oz == 1) val = v[b - 1];
-            e[h] = val;
-          }
-          dst[q] = make_float4(e[0], e[1], e[2], e[3]);
-        }
-      }
-    }
-    // runs of equal z0 (the chunk is sorted by z0): rs[z] = first lane with z0 >= z
-    int rs[9];
-#pragma unroll
-    for (int z = 0; z <= 8; ++z) rs[z] = __popc(__ballot_sync(0xffffffffu, z0 < z));
-    // z range the chunk touches: first z0 .. last z0 + W
-    const int zlo = __shfl_sync(0xffffffffu, z0, 0), zhi = __shfl_sync(0xffffffffu, z0, np_cur - 1) + W;
-    __syncwarp();
-
-#pragma unroll 1
-    for (int ri = 0; ri < P::RITER; ++ri) {
-      int bx[RPL], by[RPL];
-      bool ok[RPL];
-#pragma unroll
-      for (int q = 0; q < RPL; ++q) {
-        const int row = lane + 32 * (ri * RPL + q);
-        ok[q] = row < P::ROWS;
-        // rows past the column read the zero slot BOXP - 1 of the x vector
-        bx[q] = ok[q] ? row / P::BOX : BOXP - 1;
-        by[q] = ok[q] ? row - (row / P::BOX) * P::BOX : 0;
-      }
-      // real and imaginary accumulators of the row's z values, as aligned pairs
-      float2 ar[RPL][P::NPAIR], ai[RPL][P::NPAIR];
-#pragma unroll
-      for (int q = 0; q < RPL; ++q)
-#pragma unroll
-        for (int z = 0; z < P::NPAIR; ++z) ar[q][z] = ai[q][z] = make_float2(0.f, 0.f);
+      // runs of equal z0 (a chunk is sorted by z0): nodes [j0, j1) start at zz
+      int j1 = __popc(__ballot_sync(0xffffffffu, z0 < 1));
+      int j0 = 0;
 #pragma unroll
       for (int zz = 0; zz < 8; ++zz) {
+        if (zz > 0) {
+          j0 = j1;
+          j1 = __popc(__ballot_sync(0xffffffffu, z0 < zz + 1));
+        }
         // window start zz: taps in pairs zz/2 .. zz/2 + npr - 1
         const int b = zz >> 1, npr = (zz & 1) ? W / 2 + 1 : W / 2;
 #pragma unroll 1
-        for (int j = rs[zz]; j < rs[zz + 1]; ++j) {
-          // 8-byte broadcast reads: a warp-wide 16-byte read of one address
-          // costs four shared-memory wavefronts, an 8-byte read one
+        for (int j = j0; j < j1; ++j) {
+          const char *nd = reinterpret_cast<const char *>(wsc + j * NF);
+          // 8-byte broadcast reads (one shared-memory wavefront each)
           float2 w[P::ZP / 2];
-          const float2 *src = reinterpret_cast<const float2 *>(wz + j * P::ZP);
 #pragma unroll
           for (int k = 0; k < P::ZP / 2; ++k)
-            if (k < npr) w[k] = src[k];
+            if (k < npr) w[k] = reinterpret_cast<const float2 *>(nd + 4 * P::NZ)[k];
 #pragma unroll
-          for (int q = 0; q < RPL; ++q) {
-            const float2 xf = wxf[j * BOXP + bx[q]];
-            const float yv = wy[j * BOXP + by[q]];
+          for (int q = 0; q < RQ; ++q) {
+            const float2 xf = *reinterpret_cast<const float2 *>(nd + xo[q]);
+            const float yv = *reinterpret_cast<const float *>(nd + yo[q]);
             const float hr = xf.x * yv, hi = xf.y * yv;
             const float2 hr2 = make_float2(hr, hr), hi2 = make_float2(hi, hi);
 #pragma unroll
@@ -368,44 +383,67 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
           }
         }
       }
-#pragma unroll
-      for (int q = 0; q < RPL; ++q)
-        if (ok[q]) c3_flush_row<EXT, P::NPAIR, 6>(sg + (2 * s0 + bx[q]) * g.sx2 + (2 * s1 + by[q]) * g.sy2, ar[q],
-                                                  ai[q], zlo, zhi);
+      pair_sync(pair);  // both warps are done with the node records
+      if (last) break;
+      off = off2;
     }
-    __syncwarp();
+    // ---- flush the segment's rows into the subgrid, two cells at a time
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int row = lane + 32 * (2 * half + q);
+      if (row >= P::ROWS) continue;
+      const int bx = row / BOX, by = row - bx * BOX;
+      float2 *const rowp = sg + (2 * s0 + bx) * SX + (2 * s1 + by) * SY;
+      const unsigned ra = smem_u32(rowp);
+      constexpr int PB = 3;  // cell pairs read before the first swap
+#pragma unroll
+      for (int p0 = 0; p0 < P::NPAIR; p0 += PB) {
+        if (2 * (p0 + PB) <= zlo || 2 * p0 >= zhi) continue;
+        float4 cur[PB], add[PB];
+#pragma unroll
+        for (int e = 0; e < PB; ++e)
+          if (p0 + e < P::NPAIR) {
+            cur[e] = lds_v4_volatile(ra + 16 * (p0 + e));
+            add[e] = make_float4(ar[q][p0 + e].x, ai[q][p0 + e].x, ar[q][p0 + e].y, ai[q][p0 + e].y);
+          }
+        unsigned miss = 0;
+#pragma unroll
+        for (int e = 0; e < PB; ++e)
+          if (p0 + e < P::NPAIR) {
+            const float2 s01 = __fadd2_rn(make_float2(cur[e].x, cur[e].y), make_float2(add[e].x, add[e].y));
+            const float2 s23 = __fadd2_rn(make_float2(cur[e].z, cur[e].w), make_float2(add[e].z, add[e].w));
+            if (!cas128_shared(ra + 16 * (p0 + e), cur[e], make_float4(s01.x, s01.y, s23.x, s23.y)))
+              miss |= 1u << e;
+          }
+        if (miss) {
+#pragma unroll
+          for (int e = 0; e < PB; ++e)
+            if (p0 + e < P::NPAIR && ((miss >> e) & 1u)) {
+              float *fp = reinterpret_cast<float *>(rowp + 2 * (p0 + e));
+              atomicAdd(fp + 0, add[e].x);
+              atomicAdd(fp + 1, add[e].y);
+              atomicAdd(fp + 2, add[e].z);
+              atomicAdd(fp + 3, add[e].w);
+            }
+        }
+      }
+    }
     task = ntaskid;
     c = c2;
     a = a2;
     np = np2;
   }
   __syncthreads();
-  // ---- write-back.  A tile whose padded box lies inside the grid: the box
-  // goes densely (rows of ZB complex values, the last one zero where EXT is
-  // odd) into the warps' scratch, then one TMA add-reduce adds it to the grid.
-  constexpr int ZB = (EXT + 1) & ~1;
-  static_assert((size_t)EXT * EXT * ZB * 2 <= (size_t)C3_WARPS * P::WARP_FLOATS,
-                "the dense padded tile fits in the warps' scratch");
-  if (use_tma && org[0] + EXT <= g.n[0] && org[1] + EXT <= g.n[1] && org[2] + EXT <= g.n[2] &&
-      (smem_u32(base) & 127u) == 0) {
-    float2 *const stg = reinterpret_cast<float2 *>(base);
-    for (int r = threadIdx.x; r < EXT * EXT; r += C3_THREADS) {
-      const int c0 = r / EXT, c1 = r - c0 * EXT;
-      const float2 *src = sg + c0 * g.sx2 + c1 * g.sy2;
-      float4 *dst = reinterpret_cast<float4 *>(stg + r * ZB);
-#pragma unroll
-      for (int z = 0; z < ZB; z += 2) {
-        const float2 a = src[z];
-        const float2 b = z + 1 < EXT ? src[z + 1] : make_float2(0.f, 0.f);
-        dst[z >> 1] = make_float4(a.x, a.y, b.x, b.y);
-      }
-    }
+  // ---- write-back.  A tile whose box lies inside the grid: one TMA
+  // add-reduce straight from the subgrid (its cells past EXT add zeros).
+  if (use_tma && org[0] + EXT <= g.n[0] && org[1] + B::EXTY <= g.n[1] && org[2] + B::ZB <= g.n[2] &&
+      (smem_u32(sg) & 127u) == 0) {
     fence_proxy_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-      tma_reduce_add_3d(&gmap, stg, 2 * org[2], org[1], org[0]);
+      tma_reduce_add_3d(&gmap, sg, 2 * org[2], org[1], org[0]);
       bulk_commit();
-      bulk_wait_read_all();  // the scratch stays allocated until the copy has read it
+      bulk_wait_read_all();  // the subgrid stays allocated until the copy has read it
     }
     return;
   }
@@ -414,7 +452,7 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   for (int idx = threadIdx.x; idx < EXT * EXT * EXT; idx += C3_THREADS) {
     const int c2 = idx % EXT, r = idx / EXT;
     const int c1 = r % EXT, c0 = r / EXT;
-    const float2 v = sg[c0 * g.sx2 + c1 * g.sy2 + c2];
+    const float2 v = sg[c0 * SX + c1 * SY + c2];
     if (v.x == 0.f && v.y == 0.f) continue;
     int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
     while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
@@ -456,11 +494,10 @@ struct S3 {
   static constexpr int RITER = (ROWS + 32 * RPL - 1) / (32 * RPL);
   static constexpr int WARP_FLOATS = 3 * S3_PM * BOXP;  // wx, wy, wz [S3_PM][BOXP]
   static constexpr int INTS = 65 + 1;                   // sub-cell starts, task counter
-  // the TMA box of the padded subgrid: rows of ZB (even: 16-byte rows) complex
-  // cells, EXTY rows per x-plane -- EXT rounded up to 3 mod 8, so that the
-  // row-per-thread de-interleave reads consecutive rows from different banks
-  static constexpr int ZB = (EXT + 1) & ~1;
-  static constexpr int EXTY = EXT + ((11 - EXT % 8) % 8);
+  // the TMA box of the padded subgrid (Box3): its EXTY rows per x-plane let
+  // the row-per-thread de-interleave read consecutive rows from different banks
+  static constexpr int ZB = Box3<W>::ZB;
+  static constexpr int EXTY = Box3<W>::EXTY;
   static_assert(BOXP > BOX, "the x vector needs one zero slot past the box");
 };
 

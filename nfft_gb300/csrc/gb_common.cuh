@@ -59,7 +59,6 @@ struct Geom {
   int csz;               // sub-cell edge along the last dimension (z-column kernels: 1)
   int sub;               // sub-cells per tile ((T/cs)^(d-1) (T/csz), 1 = off)
   int sx, sy;            // shared-memory plane strides of the group kernels (x, y)
-  int sx2, sy2;          // the same for subgrids of interleaved complex values
 };
 
 // Polynomial form of the Kaiser-Bessel window (single-precision 3-D

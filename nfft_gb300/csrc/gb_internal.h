@@ -80,18 +80,17 @@ struct Col3Bufs {
   const float4 *rec;    // per sorted node: s_0, s_1, s_2, packed window starts in the tile
   const uint16_t *cst;  // per work item: 17 column starts
   const uint16_t *sst;  // per work item: 65 sub-cell starts
-  // TMA views of the oversampled grid as f32 [n_0][n_1][2 n_2] with a box of
-  // the padded tile: ext x ext_y x 2 zb floats, zb = ext rounded up to even;
-  // B^T's with ext_y = ext, B's with ext_y = S3<w>::EXTY (see gb_col3.cuh).
-  // Null where they could not be encoded (the kernels then use plain loads).
+  // TMA view of the oversampled grid as f32 [n_0][n_1][2 n_2] with a box of
+  // the padded tile: ext x ext_y x 2 zb floats, zb = ext rounded up to even,
+  // ext_y = col3_box_ext_y(w) (Box3 in gb_col3.cuh).  Null where it could
+  // not be encoded (the kernels then use plain loads and reductions).
   const CUtensorMap *grid_map;
-  const CUtensorMap *grid_map_b;
 };
 // Encodes such a view for a plan's grid (false: not representable, e.g. an
 // odd n_2, whose rows are not 16-byte multiples).
 bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ext_y);
-// y extent of B's staged subgrid for window width w (3-D single precision)
-int col3_b_ext_y(int w);
+// y extent of the 3-D column kernels' subgrid box for window width w
+int col3_box_ext_y(int w);
 // Device-side wait time-outs recorded since the last call (bounded waits on
 // TMA copies; non-zero means a copy did not arrive and the kernel gave up).
 unsigned long long read_wait_timeouts();

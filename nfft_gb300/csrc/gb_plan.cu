@@ -78,8 +78,7 @@ struct Ctx {
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
-  CUtensorMap grid_map;      // TMA views of `grid` for the 3-D column kernels (B^T, B)
-  CUtensorMap grid_map_b;
+  CUtensorMap grid_map;      // TMA view of `grid` for the 3-D column kernels (B^T, B)
   bool grid_map_ok = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -182,7 +181,6 @@ static void choose_tiles(Ctx<R> *c)
     Geom<R> h = g;
     for (int t = 0; t < 3; ++t) h.ext[t] = 8 + g.w - 1;
     h.sx = h.ext[0] * (h.ext[0] + 8) + 40;  // upper bound of the padded plane stride
-    h.sx2 = h.ext[0] * (h.ext[0] + 16) + 40;
     if (group3_smem_bytes<R>(h) <= 200 * 1024) {
       c->group3 = true;
       c->tiled = true;
@@ -216,29 +214,6 @@ static void choose_tiles(Ctx<R> *c)
             best = cost;
             g.sy = sy;
             g.sx = sx;
-          }
-        }
-      // interleaved complex (8-byte) rows: a warp's 64-bit accesses go out as
-      // two half-warps, whose 16 rows should fall on distinct bank pairs
-      best = 1 << 30;
-      g.sy2 = ext;
-      g.sx2 = ext * ext;
-      for (int sy = ext; sy < ext + 16; ++sy)
-        for (int sx = ext * sy; sx < ext * sy + 40; ++sx) {
-          int cost = 0;
-          for (int r0 = 0; r0 < rows; r0 += 16) {
-            int cnt[16] = {0}, worst = 0;
-            for (int l = 0; l < 16 && r0 + l < rows; ++l) {
-              const int r = r0 + l, bx = r / box, by = r % box;
-              worst = std::max(worst, ++cnt[(bx * sx + by * sy) & 15]);
-            }
-            cost += worst;
-          }
-          cost = cost * 4096 + (sx * ext);
-          if (cost < best) {
-            best = cost;
-            g.sy2 = sy;
-            g.sx2 = sx;
           }
         }
     }
@@ -440,8 +415,7 @@ static void init_help(typename Api<R>::plan *ths)
       dev_alloc<R>((void **)&c->c3rec, M * sizeof(float4));
       dev_alloc<R>((void **)&c->c3cst, cap * 17 * sizeof(uint16_t));
       dev_alloc<R>((void **)&c->c3sst, cap * 65 * sizeof(uint16_t));
-      c->grid_map_ok = encode_grid_map(&c->grid_map, c->grid, g.n, g.ext[0], g.ext[0]) &&
-                       encode_grid_map(&c->grid_map_b, c->grid, g.n, g.ext[0], col3_b_ext_y(g.w));
+      c->grid_map_ok = encode_grid_map(&c->grid_map, c->grid, g.n, g.ext[0], col3_box_ext_y(g.w));
     }
     make_fft<R>(c);
   }
@@ -580,7 +554,6 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   b.cst = c->c3cst;
   b.sst = c->c3sst;
   b.grid_map = c->grid_map_ok ? &c->grid_map : nullptr;
-  b.grid_map_b = c->grid_map_ok ? &c->grid_map_b : nullptr;
   return b;
 }
 

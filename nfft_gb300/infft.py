@@ -189,10 +189,10 @@ def time_to_tolerance(lib, single, N, x, m, y, tol=1e-5, w=None, refresh=0, max_
     timed (the steps enqueued back to back, the iterate copied back once at
     the end).  The reference's own iterative reconstructions stop on their
     residual too (applications/mri/mri2d/reconstruct_data_2d.c:123-131).
-    In single precision the two runs agree only to rounding: B^T adds the
-    window contributions with shared-memory atomics, whose order varies from
-    run to run, so the timed run's final residual can sit a fraction of a
-    percent on either side of the first run's.
+    The two runs agree only to rounding: B^T adds the window contributions
+    with atomics (in either precision), whose order varies from run to run,
+    so the timed run's final residual can sit a fraction of a percent on
+    either side of the first run's.
     Returns dict(iters, seconds, resid (the timed run's final residual),
     resid_found (the first run's at iters), reached (resid_found < tol), f)."""
     res = TrueResidual(lib, N, x, m, y)

@@ -11,7 +11,7 @@ products) achieves against it:
   without an FP64 residual refresh every 10 steps;
 * noiseless data: it brings the true relative data residual
   ||y - A f|| / ||y|| (A the FP64 transform) below 1e-5 in at most 1.5 times
-  the FP64 solver's iterations (a timed replay of those iterations ends
+  the FP64 solver's iterations (timed replays of those iterations end
   within 2 % of 1e-5: the order of B^T's atomic additions varies).  A relative image error of 1e-5 is not
   reachable on these trajectories by either precision: they leave the
   corners of the transform's domain unsampled, and even the FP64 iterates
@@ -63,9 +63,10 @@ def test_single_precision_cgnr_reaches_1e5_true_residual(gpulib):
     print("true residual 1e-5: FP64 %d steps (%.2e), FP32 %d steps (%.2e; timed replay %.2e)"
           % (r64["iters"], r64["resid"], r32["iters"], r32["resid_found"], r32["resid"]))
     assert r64["reached"] and r32["reached"]
-    assert r64["resid"] < 1e-5
-    assert r32["resid_found"] < 1e-5
-    # the timed FP32 replay repeats the same steps with a different order of
-    # B^T's atomic additions: its residual agrees to rounding, not bit for bit
+    assert r64["resid_found"] < 1e-5 and r32["resid_found"] < 1e-5
+    # the timed replays repeat the same steps with a different order of B^T's
+    # atomic additions (in both precisions): their residuals agree to
+    # rounding, not bit for bit
+    assert r64["resid"] < 1.02e-5, r64["resid"]
     assert r32["resid"] < 1.02e-5, r32["resid"]
     assert r32["iters"] <= 1.5 * r64["iters"], (r32["iters"], r64["iters"])

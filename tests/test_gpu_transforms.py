@@ -364,15 +364,19 @@ def test_repeated_calls_and_no_precompute_flags(gpulib):
     assert rel_l2(b, np.roll(a, 7)) < 1e-12
 
 
-@pytest.mark.parametrize("n", [[36, 40, 34], [40, 36, 33], [16, 16, 16], [24, 16, 40]])
-def test_3d_single_grids_with_and_without_tma_tiles(gpulib, n):
+@pytest.mark.parametrize("N,n", [([16, 16, 16], [36, 40, 34]), ([16, 16, 16], [40, 36, 33]),
+                                 ([8, 8, 8], [16, 16, 16]), ([12, 8, 20], [24, 16, 40])])
+def test_3d_single_grids_with_and_without_tma_tiles(gpulib, N, n):
     """The 3-D single-precision kernels on grids where the TMA paths do not all
     apply: an odd last grid length (no tensor map: every tile staged and
     written back cell by cell), grids smaller than the padded tile (every tile
     wraps around the grid edge) and mixes of interior and edge tiles.  Both
-    transforms against the oracle; no bounded TMA wait may have given up."""
+    transforms against the oracle; no bounded TMA wait may have given up.
+    (Oversampling stays at 2 or more: at n = N the window's Fourier
+    coefficients nearly vanish at the band edge, and even the oracle's own
+    single-precision path differs from its double-precision one by 2e3.)"""
     import ctypes as C
-    N, M, m = [16, 16, 16], 6000, 4
+    M, m = 6000, 4
     x, fh, f = seeded_case(N, M, seed=31)
     p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
     got_f, got_fh = run_both(p, x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64))

@@ -302,6 +302,10 @@ def run_gpu(args, wl):
     t0 = time.perf_counter()
     p.precompute_one_psi()
     t_pre = time.perf_counter() - t0
+    if wl["d"] == 3:  # which form of B node set-up chose for this density
+        qk = lib.nfftf_gb_b3_kernel
+        qk.restype, qk.argtypes = C.c_int, [C.c_void_p]
+        wl = dict(wl, kernels=("k_b3_col" if qk(C.addressof(p.p)) == 1 else "k_b3_cell", wl["kernels"][1]))
 
     rng = np.random.default_rng(100 + rank)
     fh_host = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)

@@ -43,6 +43,13 @@ static void run_g3(bool adjoint, const WorkItem *items, int nitems, typename Cx<
       GB_LAUNCHED("bt3_col");
       return;
     }
+    if (cb.b_column) {
+      set_smem_limit((const void *)k_b3_col<W>, cb_smem_bytes<W>());
+      k_b3_col<W><<<nitems, C3_THREADS, cb_smem_bytes<W>(), s>>>(items, grid, cb.rec, cb.cst, perm, f, g, poly, gmap,
+                                                                 use_tma);
+      GB_LAUNCHED("b3_col");
+      return;
+    }
     set_smem_limit((const void *)k_b3_cell<W>, s3_smem_bytes<W>(g));
     k_b3_cell<W><<<nitems, C3_THREADS, s3_smem_bytes<W>(g), s>>>(items, grid, cb.rec, cb.sst, perm, f, g, poly,
                                                                  gmap, use_tma);
@@ -68,7 +75,7 @@ template <> struct G3Set<float> {
   {
     switch (g.w) {
       case 8: return g3_smem_max<float, 8, G3_CS>(g);
-      case 10: return std::max({g3_smem_max<float, 10, G3_CS>(g), c3_smem_bytes<10>(), s3_smem_bytes<10>(g)});
+      case 10: return std::max({g3_smem_max<float, 10, G3_CS>(g), c3_smem_bytes<10>(), cb_smem_bytes<10>(), s3_smem_bytes<10>(g)});
       case 14: return g3_smem_max<float, 14, G3_CS>(g);
     }
     return 0;

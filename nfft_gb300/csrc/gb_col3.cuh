@@ -463,9 +463,11 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
 }
 
 // ---------------------------------------------------------------------------
-// B -- 3-D interpolation by sub-cell units: f_j = sum phi_0 phi_1 phi_2 g over
-// the window of every node (reference nfft_trafo_3d_B, nfft.c:4687-4914, with
-// nfft_trafo_3d_compute, nfft.c:4020-4265).
+// B -- 3-D interpolation: f_j = sum phi_0 phi_1 phi_2 g over the window of
+// every node (reference nfft_trafo_3d_B, nfft.c:4687-4914, with
+// nfft_trafo_3d_compute, nfft.c:4020-4265), in two forms: by sub-cell units
+// (k_b3_cell, for plans whose work items hold many nodes) and by column
+// segments (k_b3_col, below, for the others).
 //
 // The nodes of a 2x2x2 sub-cell of a tile share one (W+1)^3 box of the padded
 // subgrid.  A CTA stages its tile's padded subgrid in shared memory as real
@@ -746,6 +748,326 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
     const float im = __shfl_sync(0xffffffffu, acc[0], (2 * lane + 1) & 31);
     if (lane < np) f[perm[u0 + lane]] = make_float2(re, im);
     __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// B by column segments on warp pairs, the gather counterpart of k_bt3_col:
+// the CTA stages its tile's padded subgrid in the TMA box layout (one TMA copy
+// for a tile whose box lies inside the grid, plain loads for one that wraps
+// around the grid edge); its warp pairs take column segments from a shared
+// counter:
+//  * the lanes of a pair own the column's rows as in k_bt3_col and hold the
+//    17 + 1 complex values of each of their two rows as (re, im) register pairs
+//    for the whole segment;
+//  * per chunk of 32 nodes, lane j of the pair's first warp evaluates node j's
+//    x window, lane j of its second warp the y window and the z window as
+//    (w, w) pairs;
+//  * per node (a compile-time window start z0 per run, as in k_bt3_col) each
+//    row's z sum is W paired FMAs of (w, w) with (re, im) in two chains; the
+//    lane's two rows are weighted by x y and summed, the two halves of each
+//    warp are folded by one shuffle, and the 32 partial sums of the node go
+//    to shared memory;
+//  * at the end of a chunk lanes l and l + 16 of each warp sum sixteen
+//    partials of one node each, fold them and write f_j through the node
+//    permutation.
+template <int W>
+struct CB {
+  static constexpr int BOX = W + 1;
+  static constexpr int BOXP = (BOX + 3) / 4 * 4;
+  static constexpr int ROWS = BOX * BOX;
+  static constexpr int RQ = 2;
+  static constexpr int NZC = 2 * (Box3<W>::ZB / 2);  // z cells of a row held in registers
+  // per-node record (floats): x [BOXP] | y [BOXP] | z taps as (w, w) pairs [W]
+  static constexpr int NX = 0, NY = BOXP, NZ = 2 * BOXP, NF = 2 * BOXP + 2 * W;
+  static constexpr int RS = 33;  // partial sums per node (32) and one pad, complex
+  static constexpr size_t PAIR_BYTES =
+      (size_t)NF * C3_CHUNK * sizeof(float) + (size_t)C3_CHUNK * RS * sizeof(float2);
+  static_assert(NZC >= Box3<W>::EXT, "z cells cover the padded tile");
+};
+
+// subgrid box | per pair: node records, partial sums | ints | barrier
+template <int W>
+inline size_t cb_smem_bytes()
+{
+  return C3<W>::SUBGRID + (size_t)C3_PAIRS * CB<W>::PAIR_BYTES + (17 + 1 + C3_PAIRS + 3) * sizeof(int) + 8;
+}
+
+template <int W>
+__global__ void __launch_bounds__(C3_THREADS, 2) k_b3_col(const WorkItem *__restrict__ items,
+                                                           const float2 *__restrict__ grid,
+                                                           const float4 *__restrict__ rec,
+                                                           const uint16_t *__restrict__ cst,
+                                                           const uint32_t *__restrict__ perm,
+                                                           float2 *__restrict__ f, Geom<float> g, WinPoly poly,
+                                                           const __grid_constant__ CUtensorMap gmap, int use_tma)
+{
+  typedef CB<W> P;
+  typedef Box3<W> B;
+  constexpr int EXT = B::EXT, BOX = P::BOX, BOXP = P::BOXP, RQ = P::RQ, NF = P::NF, SX = B::SX, SY = B::SY;
+  extern __shared__ __align__(128) unsigned char c3_smem[];
+  float2 *const sg = reinterpret_cast<float2 *>(c3_smem);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pair = warp >> 1, half = warp & 1;
+  unsigned char *const pscr = c3_smem + C3<W>::SUBGRID + pair * P::PAIR_BYTES;
+  float *const wsc = reinterpret_cast<float *>(pscr);
+  float2 *const red = reinterpret_cast<float2 *>(pscr + (size_t)NF * C3_CHUNK * sizeof(float));
+  int *const cstart = reinterpret_cast<int *>(c3_smem + C3<W>::SUBGRID + C3_PAIRS * P::PAIR_BYTES);
+  int *const taskctr = cstart + 17;
+  int *const nextslot = taskctr + 1 + pair;
+  unsigned long long *const bar = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<uintptr_t>(taskctr + 1 + C3_PAIRS + 2) & ~(uintptr_t)7);
+
+  const WorkItem it = items[blockIdx.x];
+  int org[3];
+  {
+    int rem = it.tile;
+#pragma unroll
+    for (int t = 2; t >= 0; --t) {
+      org[t] = (rem % g.ntile[t]) * 8;
+      rem /= g.ntile[t];
+    }
+  }
+  if (threadIdx.x == 0) {
+    c3_prefetch_l2(rec + it.start, 16LL * (it.end - it.start));
+    c3_prefetch_l2(perm + it.start, 4LL * (it.end - it.start));
+  }
+  // the padded subgrid: one TMA copy where the box lies inside the grid,
+  // plain loads where it wraps around the grid edge (the cells past EXT then
+  // read as zeros; their weights are zero either way)
+  const bool tma = use_tma && org[0] + EXT <= g.n[0] && org[1] + B::EXTY <= g.n[1] && org[2] + B::ZB <= g.n[2] &&
+                   (smem_u32(sg) & 127u) == 0;
+  if (threadIdx.x == 0 && tma) {
+    mbar_init(bar, 1);
+    mbar_expect_tx(bar, (unsigned)B::BYTES);
+    tma_load_3d(sg, &gmap, 2 * org[2], org[1], org[0], bar);
+  }
+  if (!tma) {
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < EXT * EXT * B::ZB; idx += C3_THREADS) {
+      const int c2 = idx % B::ZB, r = idx / B::ZB;
+      const int c1 = r % EXT, c0 = r / EXT;
+      float2 v = make_float2(0.f, 0.f);
+      if (c2 < EXT) {
+        int p0 = org[0] + c0, p1 = org[1] + c1, p2 = org[2] + c2;
+        while (p0 >= g.n[0]) p0 -= g.n[0];  // a padded tile can wrap more than once on small grids
+        while (p1 >= g.n[1]) p1 -= g.n[1];
+        while (p2 >= g.n[2]) p2 -= g.n[2];
+        v = grid[((long long)p0 * g.n[1] + p1) * g.n[2] + p2];
+      }
+      sg[c0 * SX + c1 * SY + c2] = v;
+    }
+  }
+  if (threadIdx.x < 17) cstart[threadIdx.x] = cst[17LL * blockIdx.x + threadIdx.x];
+  if (threadIdx.x == 0) *taskctr = 0;
+  __syncthreads();
+  if (tma) {
+    // a bounded wait: a copy that never arrives costs this tile, not a hang
+    const bool ok = mbar_wait(bar, 0, TMA_WAIT_POLLS);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicAdd(&g_tma_wait_timeouts, 1ull);
+      return;
+    }
+  }
+
+  int nseg = 0;
+  if (lane < 16) nseg = (cstart[lane + 1] - cstart[lane] + C3_SEGN - 1) / C3_SEGN;
+  int incl = nseg;
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int ntask = __shfl_sync(0xffffffffu, incl, 15);
+  auto locate = [&](int task, int &c, int &a, int &np) {
+    c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
+    const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);
+    const int before = c > 0 ? prev : 0;
+    const int clen = cstart[c + 1] - cstart[c];
+    const int ns = (clen + C3_SEGN - 1) / C3_SEGN;
+    const int k = task - before, qn = clen / ns, rq = clen - qn * ns;
+    a = it.start + cstart[c] + k * qn + min(k, rq);
+    np = qn + (k < rq ? 1 : 0);
+  };
+
+  // byte offsets of the lane's rows' x and y weights in a node record (rows
+  // past the column read the zero slot BOXP - 1 of the x vector)
+  int xo[RQ], yo[RQ];
+#pragma unroll
+  for (int q = 0; q < RQ; ++q) {
+    const int row = lane + 32 * (2 * half + q);
+    const bool ok = row < P::ROWS;
+    const int bx = ok ? row / BOX : 0, by = ok ? row - (row / BOX) * BOX : 0;
+    xo[q] = 4 * P::NX + 4 * (ok ? bx : BOXP - 1);
+    yo[q] = 4 * P::NY + 4 * by;
+  }
+
+  if (half == 0 && lane == 0) *nextslot = atomicAdd(taskctr, 1);
+  pair_sync(pair);
+  int task = *nextslot;
+  pair_sync(pair);
+  int c = 0, a = 0, np = 0;
+  float4 rn = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t pn = 0;
+  if (task < ntask) {
+    locate(task, c, a, np);
+    if (lane < min(np, C3_CHUNK)) {
+      rn = rec[a + lane];
+      pn = perm[a + lane];
+    }
+  }
+  while (task < ntask) {
+    const int s0 = c >> 2, s1 = c & 3;
+    // the rows' grid values as (re, im) pairs
+    float2 gv[RQ][P::NZC];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int row = lane + 32 * (2 * half + q);
+      const int rr = row < P::ROWS ? row : 0;
+      const int bx = rr / BOX, by = rr - bx * BOX;
+      const float2 *rowp = sg + (2 * s0 + bx) * SX + (2 * s1 + by) * SY;
+#pragma unroll
+      for (int z = 0; z < P::NZC; ++z) gv[q][z] = rowp[z];
+    }
+    int off = 0;
+    int ntaskid = task, c2 = c, a2 = a, np2 = np;
+    for (;;) {
+      const float4 r = rn;
+      const uint32_t pj = pn;
+      const int npc = min(C3_CHUNK, np - off);
+      int off2 = off + C3_CHUNK;
+      const bool last = off2 >= np;  // the segment's last chunk: the next is the next task's first
+      if (last && half == 0 && lane == 0) *nextslot = atomicAdd(taskctr, 1);
+      // ---- set-up: lane j evaluates node j's windows, x in the pair's first
+      // warp, y and z in its second
+      const int loc = __float_as_int(r.w);
+      int z0 = 8;
+      if (lane < npc) {
+        float *nd = wsc + lane * NF;
+        float v[W];
+        z0 = loc >> 6;
+        if (half == 0) {
+          const int ox = (loc & 7) - 2 * s0;
+          kb_poly_taps_sym<W>(r.x, poly.c[0], v);
+          float4 *dst = reinterpret_cast<float4 *>(nd + P::NX);
+#pragma unroll
+          for (int q = 0; q < BOXP / 4; ++q) {
+            float e[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              const int b = 4 * q + h;
+              float val = 0.f;
+              if (b < W && ox == 0) val = v[b];
+              if (b >= 1 && b - 1 < W && ox == 1) val = v[b - 1];
+              e[h] = val;
+            }
+            dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+          }
+        } else {
+          const int oy = ((loc >> 3) & 7) - 2 * s1;
+          kb_poly_taps_sym<W>(r.y, poly.c[1], v);
+          {
+            float4 *dst = reinterpret_cast<float4 *>(nd + P::NY);
+#pragma unroll
+            for (int q = 0; q < BOXP / 4; ++q) {
+              float e[4];
+#pragma unroll
+              for (int h = 0; h < 4; ++h) {
+                const int b = 4 * q + h;
+                float val = 0.f;
+                if (b < W && oy == 0) val = v[b];
+                if (b >= 1 && b - 1 < W && oy == 1) val = v[b - 1];
+                e[h] = val;
+              }
+              dst[q] = make_float4(e[0], e[1], e[2], e[3]);
+            }
+          }
+          kb_poly_taps_sym<W>(r.z, poly.c[2], v);
+          float4 *dst = reinterpret_cast<float4 *>(nd + P::NZ);
+#pragma unroll
+          for (int q = 0; q < W / 2; ++q) dst[q] = make_float4(v[2 * q], v[2 * q], v[2 * q + 1], v[2 * q + 1]);
+        }
+      }
+      pair_sync(pair);  // the chunk's node records are written; the next task id is posted
+      // the next chunk's node data, loaded while this one computes
+      if (last) {
+        off2 = 0;
+        ntaskid = *nextslot;
+        if (ntaskid < ntask) locate(ntaskid, c2, a2, np2);
+      }
+      if (ntaskid < ntask) {
+        const int n2 = min(C3_CHUNK, np2 - off2);
+        if (lane < n2) {
+          rn = rec[a2 + off2 + lane];
+          pn = perm[a2 + off2 + lane];
+        }
+      }
+      // runs of equal z0 (a chunk is sorted by z0): nodes [j0, j1) start at zz
+      int j1 = __popc(__ballot_sync(0xffffffffu, z0 < 1));
+      int j0 = 0;
+#pragma unroll
+      for (int zz = 0; zz < 8; ++zz) {
+        if (zz > 0) {
+          j0 = j1;
+          j1 = __popc(__ballot_sync(0xffffffffu, z0 < zz + 1));
+        }
+#pragma unroll 1
+        for (int j = j0; j < j1; ++j) {
+          const char *nd = reinterpret_cast<const char *>(wsc + j * NF);
+          float2 w[W];
+#pragma unroll
+          for (int k = 0; k < W; ++k) w[k] = reinterpret_cast<const float2 *>(nd + 4 * P::NZ)[k];
+          float pr = 0.f, pi = 0.f;
+#pragma unroll
+          for (int q = 0; q < RQ; ++q) {
+            float2 t0 = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < W; k += 2) {
+              t0 = __ffma2_rn(w[k], gv[q][zz + k], t0);
+              t1 = __ffma2_rn(w[k + 1], gv[q][zz + k + 1], t1);
+            }
+            const float2 t = __fadd2_rn(t0, t1);
+            const float wxy =
+                *reinterpret_cast<const float *>(nd + xo[q]) * *reinterpret_cast<const float *>(nd + yo[q]);
+            pr = fmaf(wxy, t.x, pr);
+            pi = fmaf(wxy, t.y, pi);
+          }
+          pr += __shfl_xor_sync(0xffffffffu, pr, 16);
+          pi += __shfl_xor_sync(0xffffffffu, pi, 16);
+          // partial 16 half + lane of node j, at slot 16 half + lane + half
+          // (lanes l and l + 16 of the summing warp read different banks)
+          if (lane < 16) red[j * P::RS + 16 * half + lane + half] = make_float2(pr, pi);
+        }
+      }
+      pair_sync(pair);  // the partial sums are stored; both warps are done with the node records
+      // node n = 16 half + (lane & 15): lanes l and l + 16 each sum sixteen
+      // partials (those of one warp), then fold
+      {
+        const int n = 16 * half + (lane & 15), hh = lane >> 4;
+        float sr = 0.f, si = 0.f;
+        if (n < npc) {
+          const float2 *src = red + n * P::RS + 16 * hh + hh;
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const float2 v = src[k];
+            sr += v.x;
+            si += v.y;
+          }
+        }
+        sr += __shfl_xor_sync(0xffffffffu, sr, 16);
+        si += __shfl_xor_sync(0xffffffffu, si, 16);
+        const uint32_t pw = __shfl_sync(0xffffffffu, pj, n);
+        if (lane < 16 && n < npc) f[pw] = make_float2(sr, si);
+      }
+      // (the next chunk stores partial sums only after its first pair
+      // barrier, which both warps reach after these reads)
+      if (last) break;
+      off = off2;
+    }
+    task = ntaskid;
+    c = c2;
+    a = a2;
+    np = np2;
   }
 }
 

@@ -85,10 +85,17 @@ struct Col3Bufs {
   // ext_y = col3_box_ext_y(w) (Box3 in gb_col3.cuh).  Null where it could
   // not be encoded (the kernels then use plain loads and reductions).
   const CUtensorMap *grid_map;
+  // B by column segments (k_b3_col) instead of sub-cell units (k_b3_cell)
+  int b_column;
 };
 // Encodes such a view for a plan's grid (false: not representable, e.g. an
 // odd n_2, whose rows are not 16-byte multiples).
 bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ext_y);
+// mean nodes per work item from which the 3-D single-precision B runs by
+// sub-cell units rather than column segments (measured on GB300: at 512 nodes
+// per item column segments take 3.79 ms against 3.97, at about 3000 sub-cell
+// units 3.47 against 3.64)
+static constexpr int B3_DENSE = 1536;
 // y extent of the 3-D column kernels' subgrid box for window width w
 int col3_box_ext_y(int w);
 // Device-side wait time-outs recorded since the last call (bounded waits on

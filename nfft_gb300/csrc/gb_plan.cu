@@ -74,6 +74,8 @@ struct Ctx {
   WinPolyD polyd = {};   // the same in double precision (2-D double-precision kernels)
   bool col2 = false;     // 2-D column kernels (nodes keyed by column)
   int comp = 0;          // compensated 2-D single-precision B^T (nfftf_gb_set_compensated), off by default
+  int b3mode = 0;        // 3-D single-precision B (nfftf_gb_set_b3_kernel): 0 by node density, 1 column segments, 2 sub-cell units
+  bool b3dense = false;  // node set-up: the work items hold B3_DENSE nodes or more on average
   void *grid_lo = nullptr;  // its error grid (n_total complex), allocated on first use
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
@@ -499,6 +501,9 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
                          : 0;
     if constexpr (std::is_same<R, float>::value)
       if (c->col3) launch_c3_setup(c->xs, g, c->items, c->nitems, k1, c->c3rec, c->c3cst, c->c3sst, s);
+    // dense work items favour B by sub-cell units (per-unit work shared by
+    // more nodes), sparse ones B by column segments
+    c->b3dense = c->nitems > 0 && (double)g.M >= (double)B3_DENSE * c->nitems;
     if (cnt != k2) {
       GB_CUDA(cudaFree(cnt));
       GB_CUDA(cudaFree(off));
@@ -554,6 +559,7 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   b.cst = c->c3cst;
   b.sst = c->c3sst;
   b.grid_map = c->grid_map_ok ? &c->grid_map : nullptr;
+  b.b_column = c->b3mode == 1 || (c->b3mode == 0 && !c->b3dense);
   return b;
 }
 
@@ -932,6 +938,28 @@ static int set_compensated(typename Api<R>::plan *ths, int mode)
   return 0;
 }
 
+// mode 0 (by node density, the default), 1 (column segments) or 2 (sub-cell
+// units) for the 3-D single-precision B; -1 returned where the plan runs no
+// such kernel
+template <typename R>
+static int set_b3_kernel(typename Api<R>::plan *ths, int mode)
+{
+  Ctx<R> *c = ctx_of<R>(ths);
+  if (!std::is_same<R, float>::value || c->direct || !c->col3 || mode < 0 || mode > 2) return -1;
+  c->b3mode = mode;
+  return 0;
+}
+
+// the B kernel the plan runs now: 1 column segments, 2 sub-cell units, -1 none
+// of these
+template <typename R>
+static int b3_kernel(typename Api<R>::plan *ths)
+{
+  Ctx<R> *c = ctx_of<R>(ths);
+  if (!std::is_same<R, float>::value || c->direct || !c->col3) return -1;
+  return col3_bufs(c).b_column ? 1 : 2;
+}
+
 template <typename R>
 static int set_stream(typename Api<R>::plan *ths, void *stream)
 {
@@ -1014,6 +1042,8 @@ extern "C" {
   void X##finalize(X##plan *ths) { finalize<R>(ths); }                                             \
   int X##gb_set_stream(X##plan *ths, void *stream) { return set_stream<R>(ths, stream); }          \
   int X##gb_set_compensated(X##plan *ths, int mode) { return set_compensated<R>(ths, mode); }      \
+  int X##gb_set_b3_kernel(X##plan *ths, int mode) { return set_b3_kernel<R>(ths, mode); }          \
+  int X##gb_b3_kernel(X##plan *ths) { return b3_kernel<R>(ths); }                                    \
   void *X##gb_get_stream(X##plan *ths) { return (void *)ctx_of<R>(ths)->stream; }                  \
   void *X##gb_device_f_hat(X##plan *ths) { return (void *)ctx_of<R>(ths)->fhat_dev; }              \
   void *X##gb_device_f(X##plan *ths) { return (void *)ctx_of<R>(ths)->f_dev; }                     \

@@ -390,3 +390,43 @@ def test_3d_single_grids_with_and_without_tma_tiles(gpulib, N, n):
     fn = gpulib.nfft_gb_tma_wait_timeouts
     fn.restype = C.c_ulonglong
     assert fn() == 0
+
+
+@pytest.mark.parametrize("M", [6000, 300000])
+def test_3d_single_b_kernels_against_oracle(gpulib, M):
+    """Both kernels of the single-precision 3-D B (nfftf_gb_set_b3_kernel:
+    column segments and sub-cell units) against the oracle on the same plan,
+    at sparse (94 nodes per 8^3 tile) and dense (4688) nodes; the default
+    choice follows the density (column segments below 1536 nodes per work
+    item, sub-cell units above)."""
+    import ctypes as C
+    N, n, m = [16, 16, 16], [32, 32, 32], 4
+    x, fh, _ = seeded_case(N, M, seed=41)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    p.x[:] = x.astype(np.float32)
+    p.precompute_one_psi()
+    pa = C.addressof(p.p)
+    get = gpulib.nfftf_gb_b3_kernel
+    get.restype, get.argtypes = C.c_int, [C.c_void_p]
+    setk = gpulib.nfftf_gb_set_b3_kernel
+    setk.restype, setk.argtypes = C.c_int, [C.c_void_p, C.c_int]
+    assert get(pa) == (1 if M < 1536 * 64 else 2)
+    o = oracle.OraclePlan(N, M, n=n, m=m)
+    o.set_nodes(x.astype(np.float32).astype(np.float64))
+    o.precompute()
+    want = o.trafo(fh.astype(np.complex64).astype(np.complex128))
+    o.close()
+    got = {}
+    for mode in (1, 2):
+        assert setk(pa, mode) == 0 and get(pa) == mode
+        p.f_hat[:] = fh.astype(np.complex64)
+        p.trafo()
+        got[mode] = p.f.astype(np.complex128)
+    p.finalize()
+    e1, e2 = rel_l2(got[1], want), rel_l2(got[2], want)
+    print("M=%d: column segments %.2e, sub-cell units %.2e relative l2 to the oracle" % (M, e1, e2))
+    assert e1 < 1e-5 and e2 < 1e-5, (e1, e2)
+    assert rel_l2(got[1], got[2]) < 1e-5
+    fn = gpulib.nfft_gb_tma_wait_timeouts
+    fn.restype = C.c_ulonglong
+    assert fn() == 0

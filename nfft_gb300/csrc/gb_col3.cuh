@@ -770,7 +770,9 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_cell(const WorkItem *__res
 //    to shared memory;
 //  * at the end of a chunk lanes l and l + 16 of each warp sum sixteen
 //    partials of one node each, fold them and write f_j through the node
-//    permutation.
+//    permutation;
+//  * the pairs take a tile's columns longest first, so that its last
+//    segments are short.
 template <int W>
 struct CB {
   static constexpr int BOX = W + 1;
@@ -870,8 +872,30 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_col(const WorkItem *__rest
     }
   }
 
+  // columns ordered by length, longest first (16-lane bitonic sort of
+  // (length, column)): the pairs take the long columns first, so that the
+  // tile's last segments are short ones (measured: 3.83 -> 3.70 ms at 512
+  // nodes per tile; B^T, whose flushes then overlap differently, lost by it)
+  int ckey = -1, ccol = lane;
+  if (lane < 16) ckey = cstart[lane + 1] - cstart[lane];
+#pragma unroll
+  for (int k = 2; k <= 16; k <<= 1) {
+#pragma unroll
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      const int pk = __shfl_xor_sync(0xffffffffu, ckey, jj);
+      const int pc = __shfl_xor_sync(0xffffffffu, ccol, jj);
+      const bool lower = (lane & jj) == 0;
+      const bool desc = (lane & k) == 0;
+      // descending blocks keep the larger key in the lower lane
+      const bool take = desc ? (lower ? pk > ckey : pk < ckey) : (lower ? pk < ckey : pk > ckey);
+      if (lane < 16 && take) {
+        ckey = pk;
+        ccol = pc;
+      }
+    }
+  }
   int nseg = 0;
-  if (lane < 16) nseg = (cstart[lane + 1] - cstart[lane] + C3_SEGN - 1) / C3_SEGN;
+  if (lane < 16) nseg = (ckey + C3_SEGN - 1) / C3_SEGN;
   int incl = nseg;
 #pragma unroll
   for (int o = 1; o < 16; o <<= 1) {
@@ -880,9 +904,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_b3_col(const WorkItem *__rest
   }
   const int ntask = __shfl_sync(0xffffffffu, incl, 15);
   auto locate = [&](int task, int &c, int &a, int &np) {
-    c = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
-    const int prev = __shfl_sync(0xffffffffu, incl, (c + 31) & 31);
-    const int before = c > 0 ? prev : 0;
+    const int pos = __popc(__ballot_sync(0xffffffffu, lane < 16 && incl <= task));
+    const int prev = __shfl_sync(0xffffffffu, incl, (pos + 31) & 31);
+    const int before = pos > 0 ? prev : 0;
+    c = __shfl_sync(0xffffffffu, ccol, pos);
     const int clen = cstart[c + 1] - cstart[c];
     const int ns = (clen + C3_SEGN - 1) / C3_SEGN;
     const int k = task - before, qn = clen / ns, rq = clen - qn * ns;

@@ -425,7 +425,9 @@ def run_gpu(args, wl):
             "config": config_of(wl), "parallelism": "replicas x%d" % world,
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                    "ms_per_step_median": float(np.median(e2e_times)) * 1e3,
+                    "ms_per_step_min": float(np.min(e2e_times)) * 1e3},
             "clocks": clk, "gpu_launches": launches,
             "stages_ms": {k: round(v, 4) for k, v in stage.items()},
             "pair_hbm_gbs_algorithmic": round(hbm_pair, 1),

@@ -7,7 +7,7 @@ products) achieves against it:
 
 * noisy data (40 dB): after K steps its error against the phantom is within
   10 % of the FP64 solver's (CGNR on noisy data semi-converges, so both are
-  judged against the phantom, not against each other's iterate), with and
+  compared with the phantom, not with each other's iterate), with and
   without an FP64 residual refresh every 10 steps;
 * noiseless data: it brings the true relative data residual
   ||y - A f|| / ||y|| (A the FP64 transform) below 1e-5 in at most 1.5 times

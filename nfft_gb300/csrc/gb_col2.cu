@@ -5,8 +5,86 @@
 #include <algorithm>
 
 #include "gb_col2.cuh"
+#include "gb_tma.cuh"
 
 namespace gb {
+
+// bounded TMA waits that gave up (read and cleared with the 3-D kernels' count
+// by read_wait_timeouts)
+__device__ unsigned long long g_tma_wait_timeouts_2d;
+
+unsigned long long read_wait_timeouts_2d()
+{
+  unsigned long long v = 0, z = 0;
+  GB_CUDA(cudaMemcpyFromSymbol(&v, g_tma_wait_timeouts_2d, sizeof(v)));
+  GB_CUDA(cudaMemcpyToSymbol(g_tma_wait_timeouts_2d, &z, sizeof(z)));
+  return v;
+}
+
+// The per-plan single-precision B with a TMA copy of the subgrid: the
+// subgrid in the layout of one box of the grid's 2-D tensor map, EXT rows of
+// ZB complex cells (ZB = EXT rounded up to even, so that rows are 16-byte
+// multiples; the cells past EXT are not read), at the start of shared memory,
+// the warps' vectors after it.  A tile whose box lies inside the grid is
+// staged by one TMA copy (cp.async.bulk.tensor, an mbarrier with the box's
+// byte count, a bounded wait), an edge tile by plain loads.  (The same layout
+// for B^T, with one TMA add-reduce as its write-back, was slower: the even
+// row stride costs its flush bank conflicts, and the box adds the zero cells
+// of sparse tiles, which the cell-by-cell write-back skips.)
+template <int W>
+struct C2T {
+  static constexpr int EXT = C2<W>::EXT;
+  static constexpr int ZB = (EXT + 1) & ~1;
+  static constexpr size_t SUBGRID = ((size_t)EXT * ZB * sizeof(float2) + 127) / 128 * 128;
+};
+
+template <int W>
+inline size_t c2t_smem_bytes()
+{
+  return C2T<W>::SUBGRID + (size_t)C2_WARPS * C2<W>::WARP_FLOATS_B * sizeof(float) + sizeof(unsigned long long);
+}
+
+template <int W>
+__global__ void __launch_bounds__(C2_THREADS, 3) k_b2_col_tma(const WorkItem *__restrict__ items,
+                                                               const float2 *__restrict__ grid,
+                                                               const float *__restrict__ xs,
+                                                               const uint32_t *__restrict__ perm,
+                                                               float2 *__restrict__ f, Geom<float> g, WinPoly poly,
+                                                               const __grid_constant__ CUtensorMap gmap)
+{
+  typedef C2<W> P;
+  typedef C2T<W> T;
+  constexpr int EXT = T::EXT, ZB = T::ZB;
+  extern __shared__ __align__(128) unsigned char c2_smem[];
+  float2 *const sg = reinterpret_cast<float2 *>(c2_smem);
+  float *const base = reinterpret_cast<float *>(c2_smem + T::SUBGRID);
+  const int warp = threadIdx.x >> 5;
+  float *const wx = base + warp * P::WARP_FLOATS_B;
+  float *const wy = wx + P::XS * C2_CHUNK;
+  unsigned long long *const bar =
+      reinterpret_cast<unsigned long long *>(base + C2_WARPS * P::WARP_FLOATS_B);
+  const WorkItem it = items[blockIdx.x];
+  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  const bool tma = org0 + EXT <= g.n[0] && org1 + ZB <= g.n[1] && (smem_u32(sg) & 127u) == 0;
+  if (tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      mbar_expect_tx(bar, (unsigned)(EXT * ZB * sizeof(float2)));
+      tma_load_2d(sg, &gmap, 2 * org1, org0, bar);
+    }
+    __syncthreads();
+    // a bounded wait: a copy that never arrives costs this tile, not a hang
+    const bool ok = mbar_wait(bar, 0, TMA_WAIT_POLLS);
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicAdd(&g_tma_wait_timeouts_2d, 1ull);
+      return;
+    }
+  } else {
+    c2_stage_plain<W, ZB>(sg, grid, g, org0, org1);
+    __syncthreads();
+  }
+  c2_b_nodes<W, ZB>(it, sg, xs, perm, f, g, poly, wx, wy, org0, org1);
+}
 
 // per-plan kernels: one CTA per work item
 template <int W, bool COMP>
@@ -262,8 +340,15 @@ static void run_bt2(const WorkItem *items, int nitems, float2 *grid, const float
 
 template <int W>
 static void run_b2(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
-                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s, const CUtensorMap *gmap)
 {
+  if (gmap) {
+    const size_t smem = c2t_smem_bytes<W>();
+    set_smem_limit((const void *)k_b2_col_tma<W>, smem);
+    k_b2_col_tma<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly, *gmap);
+    GB_LAUNCHED("b2_col_tma");
+    return;
+  }
   const size_t smem = c2_smem_bytes<W>(false);
   set_smem_limit((const void *)k_b2_col<W>, smem);
   k_b2_col<W><<<nitems, C2_THREADS, smem, s>>>(items, grid, xs, perm, f, g, poly);
@@ -285,6 +370,11 @@ int col2_column_width(int w)
   }
 }
 
+int col2_box_zb(int w)
+{
+  return (C2_TILE + w - 1 + 1) & ~1;  // the padded tile edge rounded up to even
+}
+
 void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
                     const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s, float2 *grid_lo)
 {
@@ -302,13 +392,13 @@ void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float
 }
 
 void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
-                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s)
+                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s, const CUtensorMap *gmap)
 {
   if (nitems <= 0) return;
   switch (g.w) {
-#define GB_C2_RUN(W)                                                \
-  case W:                                                           \
-    run_b2<W>(items, nitems, grid, xs, perm, f, g, poly, s); \
+#define GB_C2_RUN(W)                                                      \
+  case W:                                                                 \
+    run_b2<W>(items, nitems, grid, xs, perm, f, g, poly, s, gmap); \
     return;
     GB_COL2_WIDTHS(GB_C2_RUN)
 #undef GB_C2_RUN

@@ -223,24 +223,18 @@ __device__ __forceinline__ int c2_setup(const float *x, const Geom<float> &g, in
 // item's subgrid to grid.  COMP: the compensated form (subgrid error plane,
 // error-free adds into grid with the errors into grid_lo, which the caller
 // folds into grid afterwards).
-template <int W, bool COMP = false>
-__device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restrict__ grid,
-                                           const float *__restrict__ xs, const uint32_t *__restrict__ perm,
-                                           const float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
-                                           unsigned char *smem_raw, float2 *__restrict__ grid_lo = nullptr)
+// The nodes of one work item accumulated into the zeroed subgrid sg (rows of
+// SYV complex cells; sgl its error plane when COMP), each warp with its
+// vectors at wx / wy.
+template <int W, bool COMP, int SYV>
+__device__ __forceinline__ void c2_bt_nodes(const WorkItem &it, float2 *sg, float2 *sgl,
+                                            const float *__restrict__ xs, const uint32_t *__restrict__ perm,
+                                            const float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
+                                            float *wx, float *wy, int org0, int org1)
 {
   typedef C2<W> P;
-  constexpr int CX = P::CX, HP = P::HP, SY = P::SY;
-  float *const base = reinterpret_cast<float *>(smem_raw);
+  constexpr int CX = P::CX, HP = P::HP, SY = SYV;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *const wx = base + warp * P::WARP_FLOATS_T;  // real, stride XS
-  float *const wy = wx + P::XS * C2_CHUNK;
-  float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_T);
-  float2 *const sgl = sg + P::EXT * SY;  // error plane (COMP only)
-
-  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
-  for (int i = threadIdx.x; i < (COMP ? 2 : 1) * P::EXT * SY; i += C2_THREADS) sg[i] = make_float2(0.f, 0.f);
-  __syncthreads();
   const int h = lane >> 4, r = lane & 15;
 
   for (int a = it.start + warp * C2_CHUNK; a < it.end; a += C2_WARPS * C2_CHUNK) {
@@ -285,6 +279,27 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
     }
     __syncwarp();  // the next task's set-up reuses the vectors
   }
+}
+
+template <int W, bool COMP = false>
+__device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restrict__ grid,
+                                           const float *__restrict__ xs, const uint32_t *__restrict__ perm,
+                                           const float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
+                                           unsigned char *smem_raw, float2 *__restrict__ grid_lo = nullptr)
+{
+  typedef C2<W> P;
+  constexpr int SY = P::SY;
+  float *const base = reinterpret_cast<float *>(smem_raw);
+  const int warp = threadIdx.x >> 5;
+  float *const wx = base + warp * P::WARP_FLOATS_T;  // real, stride XS
+  float *const wy = wx + P::XS * C2_CHUNK;
+  float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_T);
+  float2 *const sgl = sg + P::EXT * SY;  // error plane (COMP only)
+
+  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  for (int i = threadIdx.x; i < (COMP ? 2 : 1) * P::EXT * SY; i += C2_THREADS) sg[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  c2_bt_nodes<W, COMP, SY>(it, sg, sgl, xs, perm, f, g, poly, wx, wy, org0, org1);
   __syncthreads();
   for (int idx = threadIdx.x; idx < P::EXT * P::EXT; idx += C2_THREADS) {
     const int rx = idx / P::EXT, ry = idx - rx * P::EXT;
@@ -303,29 +318,33 @@ __device__ __forceinline__ void c2_bt_item(const WorkItem &it, float2 *__restric
 
 // B of one work item by a CTA of C2_THREADS threads with c2_smem_bytes<W>(false)
 // bytes of shared memory at smem_raw; writes f of the item's nodes.
-template <int W>
-__device__ __forceinline__ void c2_b_item(const WorkItem &it, const float2 *__restrict__ grid,
-                                          const float *__restrict__ xs, const uint32_t *__restrict__ perm,
-                                          float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
-                                          unsigned char *smem_raw)
+// The padded subgrid of the tile at (org0, org1) into sg (rows of SYV complex
+// cells) by plain loads, wrapping around the grid edge.
+template <int W, int SYV>
+__device__ __forceinline__ void c2_stage_plain(float2 *sg, const float2 *__restrict__ grid, const Geom<float> &g,
+                                               int org0, int org1)
 {
-  typedef C2<W> P;
-  constexpr int CX = P::CX, HP = P::HP, SY = P::SY, EXT = P::EXT;
-  float *const base = reinterpret_cast<float *>(smem_raw);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *const wx = base + warp * P::WARP_FLOATS_B;  // real, stride XS
-  float *const wy = wx + P::XS * C2_CHUNK;
-  float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_B);
-
-  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  constexpr int EXT = C2<W>::EXT;
   for (int idx = threadIdx.x; idx < EXT * EXT; idx += C2_THREADS) {
     const int rx = idx / EXT, ry = idx - rx * EXT;
     int p0 = org0 + rx, p1 = org1 + ry;
     while (p0 >= g.n[0]) p0 -= g.n[0];
     while (p1 >= g.n[1]) p1 -= g.n[1];
-    sg[rx * SY + ry] = grid[(long long)p0 * g.n[1] + p1];
+    sg[rx * SYV + ry] = grid[(long long)p0 * g.n[1] + p1];
   }
-  __syncthreads();
+}
+
+// B of the nodes of one work item from the staged subgrid sg (rows of SYV
+// complex cells), each warp with its vectors at wx / wy.
+template <int W, int SYV>
+__device__ __forceinline__ void c2_b_nodes(const WorkItem &it, const float2 *sg, const float *__restrict__ xs,
+                                           const uint32_t *__restrict__ perm, float2 *__restrict__ f,
+                                           const Geom<float> &g, const WinPoly &poly, float *wx, float *wy,
+                                           int org0, int org1)
+{
+  typedef C2<W> P;
+  constexpr int CX = P::CX, HP = P::HP, SY = SYV, EXT = P::EXT;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int h = lane >> 4, r = lane & 15;
 
   for (int a = it.start + warp * C2_CHUNK; a < it.end; a += C2_WARPS * C2_CHUNK) {
@@ -401,6 +420,24 @@ __device__ __forceinline__ void c2_b_item(const WorkItem &it, const float2 *__re
     }
     __syncwarp();  // the next task's set-up reuses the vectors
   }
+}
+
+template <int W>
+__device__ __forceinline__ void c2_b_item(const WorkItem &it, const float2 *__restrict__ grid,
+                                          const float *__restrict__ xs, const uint32_t *__restrict__ perm,
+                                          float2 *__restrict__ f, const Geom<float> &g, const WinPoly &poly,
+                                          unsigned char *smem_raw)
+{
+  typedef C2<W> P;
+  float *const base = reinterpret_cast<float *>(smem_raw);
+  const int warp = threadIdx.x >> 5;
+  float *const wx = base + warp * P::WARP_FLOATS_B;  // real, stride XS
+  float *const wy = wx + P::XS * C2_CHUNK;
+  float2 *const sg = reinterpret_cast<float2 *>(base + C2_WARPS * P::WARP_FLOATS_B);
+  const int org0 = (it.tile / g.ntile[1]) * C2_TILE, org1 = (it.tile % g.ntile[1]) * C2_TILE;
+  c2_stage_plain<W, P::SY>(sg, grid, g, org0, org1);
+  __syncthreads();
+  c2_b_nodes<W, P::SY>(it, sg, xs, perm, f, g, poly, wx, wy, org0, org1);
 }
 
 }  // namespace gb

@@ -42,6 +42,30 @@ bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ex
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool encode_grid_map_2d(CUtensorMap *map, void *grid, const int *n, int ext, int zb)
+{
+  // rows of 2 n_1 floats must be 16-byte multiples, the box within 256 per dimension
+  if (!grid || (n[1] & 1) || (zb & 1) || ext > 256 || 2 * zb > 256) return false;
+  static std::once_flag once;
+  static EncodeTiledFn enc = nullptr;
+  std::call_once(once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      enc = (EncodeTiledFn)fn;
+  });
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)2 * n[1], (cuuint64_t)n[0]};
+  const cuuint64_t strides[1] = {(cuuint64_t)8 * n[1]};
+  const cuuint32_t box[2] = {(cuuint32_t)(2 * zb), (cuuint32_t)ext};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, grid, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 __global__ void k_c3_records(const float *__restrict__ xs, Geom<float> g, float4 *__restrict__ rec)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

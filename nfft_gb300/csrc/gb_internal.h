@@ -91,6 +91,9 @@ struct Col3Bufs {
 // Encodes such a view for a plan's grid (false: not representable, e.g. an
 // odd n_2, whose rows are not 16-byte multiples).
 bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ext_y);
+// the 2-D view f32 [n_0][2 n_1] with boxes of ext rows of zb complex values
+// (zb even); false where it cannot be encoded (odd n_1)
+bool encode_grid_map_2d(CUtensorMap *map, void *grid, const int *n, int ext, int zb);
 // mean nodes per work item from which the 3-D single-precision B runs by
 // sub-cell units rather than column segments (measured on GB300: at 512 nodes
 // per item column segments take 3.79 ms against 3.97, at about 3000 sub-cell
@@ -117,12 +120,20 @@ void launch_bt3_group(const WorkItem *items, int nitems, typename Cx<R>::T *grid
 // the width has no such kernel
 int col2_column_width(int w);
 // grid_lo non-null: the compensated form (B^T's rounding errors gathered in
-// grid_lo, n_0 n_1 complex, zeroed by the caller, then folded into grid)
+// grid_lo, n_0 n_1 complex, zeroed by the caller, then folded into grid).
+// B's gmap non-null: the grid's 2-D TMA view (encode_grid_map_2d with ext =
+// 32 + w - 1 and zb = col2_box_zb(w)); without it B stages the subgrid cell by
+// cell.
 void launch_bt2_col(const WorkItem *items, int nitems, float2 *grid, const float *xs, const uint32_t *perm,
                     const float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s,
                     float2 *grid_lo = nullptr);
 void launch_b2_col(const WorkItem *items, int nitems, const float2 *grid, const float *xs, const uint32_t *perm,
-                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s);
+                   float2 *f, const Geom<float> &g, const WinPoly &poly, cudaStream_t s,
+                   const CUtensorMap *gmap = nullptr);
+// row length (complex cells, even) of the 2-D column kernels' TMA box
+int col2_box_zb(int w);
+// bounded TMA waits of the 2-D kernels that gave up (read and cleared)
+unsigned long long read_wait_timeouts_2d();
 // the B^T of the same layout in double precision, and a per-node B on the
 // same work items (both with the window's degree-16 form)
 void launch_bt2_col_d(const WorkItem *items, int nitems, double2 *grid, const double *xs, const uint32_t *perm,

@@ -81,6 +81,8 @@ struct Ctx {
   float4 *c3rec = nullptr;
   uint16_t *c3cst = nullptr, *c3sst = nullptr;
   CUtensorMap grid_map;      // TMA view of `grid` for the 3-D column kernels (B^T, B)
+  CUtensorMap grid_map2;     // TMA view of `grid` for the 2-D single-precision column B
+  bool grid_map2_ok = false;
   bool grid_map_ok = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -419,6 +421,8 @@ static void init_help(typename Api<R>::plan *ths)
       dev_alloc<R>((void **)&c->c3sst, cap * 65 * sizeof(uint16_t));
       c->grid_map_ok = encode_grid_map(&c->grid_map, c->grid, g.n, g.ext[0], col3_box_ext_y(g.w));
     }
+    if (c->col2 && sizeof(R) == 4)
+      c->grid_map2_ok = encode_grid_map_2d(&c->grid_map2, c->grid, g.n, 32 + g.w - 1, col2_box_zb(g.w));
     make_fft<R>(c);
   }
   launch_cphi<R>(g, c->cphi, c->stream);
@@ -571,7 +575,8 @@ static bool b2_stage(Ctx<R> *c, typename Cx<R>::T *f)
 {
   if (!c->col2) return false;
   if constexpr (std::is_same<R, float>::value)
-    launch_b2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream);
+    launch_b2_col(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->poly, c->stream,
+                  c->grid_map2_ok ? &c->grid_map2 : nullptr);
   else
     launch_b2_node_d(c->items, c->nitems, c->grid, c->xs, c->perm, f, c->g, c->polyd, c->stream);
   return true;

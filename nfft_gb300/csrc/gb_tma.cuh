@@ -3,7 +3,9 @@
 //
 // The oversampled grid is viewed as a 3-D tensor of floats [n_0][n_1][2 n_2]
 // (complex values interleaved along the last dimension; encode_grid_map in
-// gb_col3_setup.cu), one box being a padded tile: ext x ext x 2 zb floats.
+// gb_col3_setup.cu), one box being a padded tile: ext x ext x 2 zb floats;
+// a 2-D grid as [n_0][2 n_1] with boxes of ext x 2 zb floats
+// (encode_grid_map_2d).
 //  * tma_load_3d copies a box into shared memory and signals an mbarrier with
 //    the byte count (B's subgrid staging);
 //  * tma_reduce_add_3d adds a box from shared memory into the grid (B^T's
@@ -42,6 +44,24 @@ __device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap *map, const 
   asm volatile("cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
                    map),
                "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+               : "memory");
+}
+
+// the same for 2-D views (the 2-D column kernels: f32 [n_0][2 n_1])
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            unsigned long long *bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap *map, const void *src, int c0, int c1)
+{
+  asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(map),
+               "r"(c0), "r"(c1), "r"(smem_u32(src))
                : "memory");
 }
 

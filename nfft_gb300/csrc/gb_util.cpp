@@ -161,7 +161,7 @@ GB_MALLOC_API(nfftf_, "nfftf_malloc")
 
 unsigned long long nfft_gb_tma_wait_timeouts(void)
 {
-  return gb::read_wait_timeouts();
+  return gb::read_wait_timeouts() + gb::read_wait_timeouts_2d();
 }
 
 const char *nfft_gb_last_error(void)

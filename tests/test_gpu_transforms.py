@@ -430,3 +430,29 @@ def test_3d_single_b_kernels_against_oracle(gpulib, M):
     fn = gpulib.nfft_gb_tma_wait_timeouts
     fn.restype = C.c_ulonglong
     assert fn() == 0
+
+
+@pytest.mark.parametrize("N,n", [([32, 32], [64, 64]), ([32, 32], [96, 66]), ([32, 32], [64, 65]),
+                                 ([16, 16], [40, 48])])
+def test_2d_single_grids_with_and_without_tma_tiles(gpulib, N, n):
+    """The 2-D single-precision column kernels on grids where B's TMA staging
+    does not always apply: an odd last grid length (no tensor map: every tile
+    staged cell by cell), grids smaller than the padded tile (every tile
+    wraps around the grid edge) and mixes of interior and edge tiles.  Both
+    transforms against the oracle; no bounded TMA wait may have given up."""
+    import ctypes as C
+    M, m = 3000, 6
+    x, fh, f = seeded_case(N, M, seed=37)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    got_f, got_fh = run_both(p, x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64))
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m)
+    o.set_nodes(x.astype(np.float32).astype(np.float64))
+    o.precompute()
+    e_t = rel_l2(got_f.astype(np.complex128), o.trafo(fh.astype(np.complex64).astype(np.complex128)))
+    e_a = rel_l2(got_fh.astype(np.complex128), o.adjoint(f.astype(np.complex64).astype(np.complex128)))
+    o.close()
+    assert e_t < 1e-5 and e_a < 1e-5, (n, e_t, e_a)
+    fn = gpulib.nfft_gb_tma_wait_timeouts
+    fn.restype = C.c_ulonglong
+    assert fn() == 0

@@ -456,3 +456,61 @@ def test_2d_single_grids_with_and_without_tma_tiles(gpulib, N, n):
     fn = gpulib.nfft_gb_tma_wait_timeouts
     fn.restype = C.c_ulonglong
     assert fn() == 0
+
+
+def _sweep_cases(count=10, seed=2024):
+    """Seeded random single-precision 3-D plans for the column kernels (m = 4):
+    N_t even in 8..40, n_t = sigma N_t with sigma in [1.5, 2.5] (odd n_t
+    included), M in 200..60000, uniform or clustered nodes."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(count):
+        N = [int(2 * rng.integers(4, 21)) for _ in range(3)]
+        n = [max(int(np.ceil(rng.uniform(1.5, 2.5) * v)), 16) for v in N]
+        M = int(rng.integers(200, 60001))
+        dist = "clustered" if rng.random() < 0.3 else "uniform"
+        cases.append((N, n, M, dist))
+    return cases
+
+
+@pytest.mark.parametrize("N,n,M,dist", _sweep_cases())
+def test_3d_single_random_plans_both_b_kernels(gpulib, N, n, M, dist):
+    """Random single-precision 3-D plans: trafo with either B kernel
+    (column segments and sub-cell units) and the adjoint, against the oracle."""
+    import ctypes as C
+    from nfft_gb300 import workloads
+    m = 4
+    rng = np.random.default_rng(M)
+    x = workloads.cube_nodes(M, 3, dist, int(M % 97)).astype(np.float64)
+    NN = int(np.prod(N))
+    fh = (rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)).astype(np.complex64)
+    f = (rng.uniform(-1, 1, M) + 1j * rng.uniform(-1, 1, M)).astype(np.complex64)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    p.x[:] = x.astype(np.float32)
+    p.precompute_one_psi()
+    pa = C.addressof(p.p)
+    setk = gpulib.nfftf_gb_set_b3_kernel
+    setk.restype, setk.argtypes = C.c_int, [C.c_void_p, C.c_int]
+    o = oracle.OraclePlan(N, M, n=n, m=m)
+    o.set_nodes(x.astype(np.float32).astype(np.float64))
+    o.precompute()
+    want_t = o.trafo(fh.astype(np.complex128))
+    want_a = o.adjoint(f.astype(np.complex128))
+    o.close()
+    errs = []
+    for mode in (1, 2):
+        if setk(pa, mode) != 0:  # a plan without the 3-D column kernels: one B only
+            continue
+        p.f_hat[:] = fh
+        p.trafo()
+        errs.append(rel_l2(p.f.astype(np.complex128), want_t))
+    p.f[:] = f
+    p.adjoint()
+    e_a = rel_l2(p.f_hat.astype(np.complex128), want_a)
+    p.finalize()
+    print(N, n, M, dist, "trafo", ["%.2e" % e for e in errs], "adjoint %.2e" % e_a)
+    assert all(e < 1e-5 for e in errs), errs
+    assert e_a < 1e-5, e_a
+    fn = gpulib.nfft_gb_tma_wait_timeouts
+    fn.restype = C.c_ulonglong
+    assert fn() == 0

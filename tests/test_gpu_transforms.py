@@ -514,3 +514,38 @@ def test_3d_single_random_plans_both_b_kernels(gpulib, N, n, M, dist):
     fn = gpulib.nfft_gb_tma_wait_timeouts
     fn.restype = C.c_ulonglong
     assert fn() == 0
+
+
+def _sweep_cases_2d(seed=2025):
+    """Seeded random single-precision 2-D plans, one per column-kernel width
+    (m = 2 ... 7, w = 2m + 2): N_t even in 32..96, n_t = sigma N_t with sigma
+    in [1.5, 2.5] (odd n_t included), M in 500..40000."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for m in range(2, 8):
+        N = [int(2 * rng.integers(16, 49)) for _ in range(2)]
+        n = [int(np.ceil(rng.uniform(1.5, 2.5) * v)) for v in N]
+        cases.append((N, n, int(rng.integers(500, 40001)), m))
+    return cases
+
+
+@pytest.mark.parametrize("N,n,M,m", _sweep_cases_2d())
+def test_2d_single_random_plans_every_width(gpulib, N, n, M, m):
+    """Random single-precision 2-D plans, every window width of the column
+    kernels: trafo and adjoint against the oracle."""
+    import ctypes as C
+    x, fh, f = seeded_case(N, M, seed=M)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    got_f, got_fh = run_both(p, x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64))
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m)
+    o.set_nodes(x.astype(np.float32).astype(np.float64))
+    o.precompute()
+    e_t = rel_l2(got_f.astype(np.complex128), o.trafo(fh.astype(np.complex64).astype(np.complex128)))
+    e_a = rel_l2(got_fh.astype(np.complex128), o.adjoint(f.astype(np.complex64).astype(np.complex128)))
+    o.close()
+    print(N, n, M, m, "trafo %.2e adjoint %.2e" % (e_t, e_a))
+    assert e_t < 1e-5 and e_a < 1e-5, (e_t, e_a)
+    fn = gpulib.nfft_gb_tma_wait_timeouts
+    fn.restype = C.c_ulonglong
+    assert fn() == 0

@@ -180,12 +180,14 @@ void nfft_gb_kb_poly_fit(int m, double b, int w, float *coef);
  * computed in extended precision and rounded to double.  Host only. */
 void nfft_gb_kb_polyd_fit(int m, double b, int w, double *coef);
 
-/* Bounded waits of the 3-D single-precision transforms that gave up since
- * the last call (no counterpart in the reference).  Their B kernel stages
- * each tile of the oversampled grid with a TMA copy and waits for it at most
- * about a second; a copy that never arrives leaves that tile's samples
- * unwritten and is counted here instead of hanging the GPU.  Reads and
- * clears the count of the current device; 0 in every correct run. */
+/* Bounded waits of the single-precision 3-D and 2-D transforms that gave up
+ * since the last call (no counterpart in the reference).  Their B kernels
+ * stage each tile of the oversampled grid with a TMA copy and wait for it at
+ * most about a second; a copy that never arrives leaves that tile's samples
+ * unwritten and is counted here instead of hanging the GPU.  The 3-D B^T
+ * adds its column segments to a tile's subgrid under a lock whose spin is
+ * bounded the same way (a segment that gives up is not added, and counted).
+ * Reads and clears the count of the current device; 0 in every correct run. */
 unsigned long long nfft_gb_tma_wait_timeouts(void);
 
 /* The node sort of NFFT_SORT_NODES without any device allocation (no

@@ -42,10 +42,13 @@
 //    them) each row takes exactly W or W + 2 paired FMAs (fma.rn.f32x2 of the
 //    sm_100 family: two z values at once);
 //  * at the end of a segment each row is added to the shared subgrid two
-//    cells at a time: a 16-byte read, two paired adds and a 128-bit
-//    compare-and-swap (atom.shared.cas.b128), all of a block's cells read
-//    before the first swap; a cell pair another warp changed in between is
-//    added again with per-component atomic adds;
+//    cells at a time (16-byte read, two paired adds, 16-byte store), one pair
+//    at a time under the CTA's flush lock: segments end thousands of cycles
+//    apart, so the lock is rarely contended, and a plain read-add-write moves
+//    about a third less shared-memory data than a compare-and-swap would
+//    (the lock's spin is bounded: a pair that gives up counts a time-out and
+//    skips its flush, so a broken lock shows as wrong sums and a non-zero
+//    nfft_gb_tma_wait_timeouts, never as a hang);
 //  * the subgrid goes to the global grid once per work item: a tile whose box
 //    lies inside the grid by one TMA add-reduce (cp.reduce.async.bulk.tensor)
 //    straight from the subgrid; a tile whose box wraps around the grid edge
@@ -58,8 +61,9 @@
 
 namespace gb {
 
-// bounded TMA waits that gave up (read and cleared by read_wait_timeouts);
-// this header is compiled into one unit (gb_b3group.cu)
+// bounded waits that gave up, on TMA copies or on B^T's flush lock (read and
+// cleared by read_wait_timeouts); this header is compiled into one unit
+// (gb_b3group.cu)
 __device__ unsigned long long g_tma_wait_timeouts;
 
 static constexpr int C3_THREADS = 256;
@@ -101,7 +105,7 @@ template <int W>
 inline size_t c3_smem_bytes()
 {
   typedef C3<W> P;
-  return P::SUBGRID + (size_t)C3_PAIRS * P::NF * C3_CHUNK * sizeof(float) + (17 + 1 + C3_PAIRS) * sizeof(int);
+  return P::SUBGRID + (size_t)C3_PAIRS * P::NF * C3_CHUNK * sizeof(float) + (17 + 2 + 2 * C3_PAIRS) * sizeof(int);
 }
 
 // Starts a bulk copy of the 16-byte aligned interior of [p, p + bytes) from
@@ -115,37 +119,6 @@ __device__ __forceinline__ void c3_prefetch_l2(const void *p, long long bytes)
     const unsigned n = (unsigned)((e - q) < (1u << 20) ? (e - q) : (1u << 20));
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
   }
-}
-
-// 16-byte shared-memory read that sees other warps' stores
-__device__ __forceinline__ float4 lds_v4_volatile(unsigned a)
-{
-  float4 v;
-  asm volatile("ld.volatile.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "r"(a));
-  return v;
-}
-
-// 128-bit compare-and-swap on shared memory (sm_90 and later); true where it
-// swapped
-__device__ __forceinline__ bool cas128_shared(unsigned a, float4 expect, float4 want)
-{
-  const unsigned long long e0 = ((unsigned long long)__float_as_uint(expect.y) << 32) | __float_as_uint(expect.x);
-  const unsigned long long e1 = ((unsigned long long)__float_as_uint(expect.w) << 32) | __float_as_uint(expect.z);
-  const unsigned long long w0 = ((unsigned long long)__float_as_uint(want.y) << 32) | __float_as_uint(want.x);
-  const unsigned long long w1 = ((unsigned long long)__float_as_uint(want.w) << 32) | __float_as_uint(want.z);
-  unsigned long long o0, o1;
-  asm volatile(
-      "{\n\t.reg .b128 e, w, o;\n\t"
-      "mov.b128 e, {%2, %3};\n\t"
-      "mov.b128 w, {%4, %5};\n\t"
-      "atom.shared.cas.b128 o, [%6], e, w;\n\t"
-      "mov.b128 {%0, %1}, o;\n\t}"
-      : "=l"(o0), "=l"(o1)
-      : "l"(e0), "l"(e1), "l"(w0), "l"(w1), "r"(a)
-      : "memory");
-  return o0 == e0 && o1 == e1;
 }
 
 // the two warps of pair p (named barrier p + 1; barrier 0 is __syncthreads)
@@ -198,7 +171,10 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
   }
   // column boundaries of the item (node set-up): cstart[c] = first node of column c
   if (threadIdx.x < 17) cstart[threadIdx.x] = cst[17LL * blockIdx.x + threadIdx.x];
-  if (threadIdx.x == 0) *taskctr = 0;
+  if (threadIdx.x == 0) {
+    *taskctr = 0;
+    taskctr[1 + C3_PAIRS] = 0;  // the flush lock
+  }
   __syncthreads();
 
   // segments per column (lanes 0..15), inclusive scan -> task -> column map
@@ -387,45 +363,48 @@ __global__ void __launch_bounds__(C3_THREADS, 2) k_bt3_col(const WorkItem *__res
       if (last) break;
       off = off2;
     }
-    // ---- flush the segment's rows into the subgrid, two cells at a time
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-      const int row = lane + 32 * (2 * half + q);
-      if (row >= P::ROWS) continue;
-      const int bx = row / BOX, by = row - bx * BOX;
-      float2 *const rowp = sg + (2 * s0 + bx) * SX + (2 * s1 + by) * SY;
-      const unsigned ra = smem_u32(rowp);
-      constexpr int PB = 3;  // cell pairs read before the first swap
-#pragma unroll
-      for (int p0 = 0; p0 < P::NPAIR; p0 += PB) {
-        if (2 * (p0 + PB) <= zlo || 2 * p0 >= zhi) continue;
-        float4 cur[PB], add[PB];
-#pragma unroll
-        for (int e = 0; e < PB; ++e)
-          if (p0 + e < P::NPAIR) {
-            cur[e] = lds_v4_volatile(ra + 16 * (p0 + e));
-            add[e] = make_float4(ar[q][p0 + e].x, ai[q][p0 + e].x, ar[q][p0 + e].y, ai[q][p0 + e].y);
+    // ---- flush the segment's rows into the subgrid under the CTA's flush lock:
+    // one pair at a time, by plain 16-byte read, paired adds and 16-byte store
+    // (measured on GB300: 3.41 ms per launch at 512 nodes per tile against
+    // 3.74 with a 128-bit compare-and-swap per cell pair and no lock)
+    {
+      int *const lockp = taskctr + 1 + C3_PAIRS;
+      int *const haveslot = lockp + 1 + pair;
+      if (half == 0 && lane == 0) {
+        int got = 0;
+        for (unsigned i = 0; i < (1u << 20); ++i) {
+          if (atomicCAS(lockp, 0, 1) == 0) {
+            got = 1;
+            break;
           }
-        unsigned miss = 0;
-#pragma unroll
-        for (int e = 0; e < PB; ++e)
-          if (p0 + e < P::NPAIR) {
-            const float2 s01 = __fadd2_rn(make_float2(cur[e].x, cur[e].y), make_float2(add[e].x, add[e].y));
-            const float2 s23 = __fadd2_rn(make_float2(cur[e].z, cur[e].w), make_float2(add[e].z, add[e].w));
-            if (!cas128_shared(ra + 16 * (p0 + e), cur[e], make_float4(s01.x, s01.y, s23.x, s23.y)))
-              miss |= 1u << e;
-          }
-        if (miss) {
-#pragma unroll
-          for (int e = 0; e < PB; ++e)
-            if (p0 + e < P::NPAIR && ((miss >> e) & 1u)) {
-              float *fp = reinterpret_cast<float *>(rowp + 2 * (p0 + e));
-              atomicAdd(fp + 0, add[e].x);
-              atomicAdd(fp + 1, add[e].y);
-              atomicAdd(fp + 2, add[e].z);
-              atomicAdd(fp + 3, add[e].w);
-            }
+          __nanosleep(64);
         }
+        __threadfence_block();
+        if (!got) atomicAdd(&g_tma_wait_timeouts, 1ull);
+        *haveslot = got;
+      }
+      pair_sync(pair);
+      if (*haveslot) {
+#pragma unroll
+        for (int q = 0; q < RQ; ++q) {
+          const int row = lane + 32 * (2 * half + q);
+          if (row >= P::ROWS) continue;
+          const int bx = row / BOX, by = row - bx * BOX;
+          float4 *const rowp = reinterpret_cast<float4 *>(sg + (2 * s0 + bx) * SX + (2 * s1 + by) * SY);
+#pragma unroll
+          for (int p = 0; p < P::NPAIR; ++p) {
+            if (2 * p + 2 <= zlo || 2 * p >= zhi) continue;
+            const float4 cur = rowp[p];
+            const float2 s01 = __fadd2_rn(make_float2(cur.x, cur.y), make_float2(ar[q][p].x, ai[q][p].x));
+            const float2 s23 = __fadd2_rn(make_float2(cur.z, cur.w), make_float2(ar[q][p].y, ai[q][p].y));
+            rowp[p] = make_float4(s01.x, s01.y, s23.x, s23.y);
+          }
+        }
+      }
+      pair_sync(pair);
+      if (half == 0 && lane == 0 && *haveslot) {
+        __threadfence_block();
+        atomicExch(lockp, 0);
       }
     }
     task = ntaskid;

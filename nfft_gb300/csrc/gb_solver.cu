@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/nfft3.h"
@@ -96,19 +97,30 @@ __global__ void k_scale_copy(typename Cx<R>::T *__restrict__ dst, const typename
   }
 }
 
-// x += sign * scal[idx] * w * y   (upd_xpay / upd_xpawy)
+// x += sign * scal[idx] * w * y   (upd_xpay / upd_xpawy).  The vector
+// updates of a single-precision solver run in single precision (the scalar
+// rounded once to float, one FMA per component): FP64 stays with the inner
+// products and norms, where it decides the iteration; GB300's FP64 rate is a
+// small fraction of its FP32 rate.
 template <typename R>
 __global__ void k_upd(typename Cx<R>::T *__restrict__ x, const typename Cx<R>::T *__restrict__ y,
                       const R *__restrict__ w, long long n, const double *__restrict__ scal, int idx,
                       double sign)
 {
   const double a = sign * scal[idx];
+  const R ar = (R)a;
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    const double c = w ? a * (double)w[k] : a;
     typename Cx<R>::T v = x[k];
     const typename Cx<R>::T u = y[k];
-    v.x = (R)((double)v.x + c * (double)u.x);
-    v.y = (R)((double)v.y + c * (double)u.y);
+    if constexpr (std::is_same<R, float>::value) {
+      const float c = w ? ar * w[k] : ar;
+      v.x = fmaf(c, u.x, v.x);
+      v.y = fmaf(c, u.y, v.y);
+    } else {
+      const double c = w ? a * (double)w[k] : a;
+      v.x = (R)((double)v.x + c * (double)u.x);
+      v.y = (R)((double)v.y + c * (double)u.y);
+    }
     x[k] = v;
   }
 }
@@ -119,11 +131,17 @@ __global__ void k_axpy(typename Cx<R>::T *__restrict__ x, const typename Cx<R>::
                        const double *__restrict__ scal, int idx)
 {
   const double a = idx >= 0 ? scal[idx] : -1.0;
+  const R ar = (R)a;
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     typename Cx<R>::T v = x[k];
     const typename Cx<R>::T u = y[k];
-    v.x = (R)(a * (double)v.x + (double)u.x);
-    v.y = (R)(a * (double)v.y + (double)u.y);
+    if constexpr (std::is_same<R, float>::value) {
+      v.x = fmaf(ar, v.x, u.x);
+      v.y = fmaf(ar, v.y, u.y);
+    } else {
+      v.x = (R)(a * (double)v.x + (double)u.x);
+      v.y = (R)(a * (double)v.y + (double)u.y);
+    }
     x[k] = v;
   }
 }
@@ -238,23 +256,36 @@ __global__ void __launch_bounds__(RED_THREADS) k_upd_dot(typename Cx<R>::T *__re
                                                          double *__restrict__ scal, int op)
 {
   const double a = scal[S_ALPHA];
+  const R ar = (R)a;
+  constexpr bool SP = std::is_same<R, float>::value;  // single precision: FP32 updates (see k_upd)
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p)
     for (long long k = k0; k < N; k += stride) {
-      const double c = wh ? a * (double)wh[k] : a;
       typename Cx<R>::T u = fh[k];
       const typename Cx<R>::T d = p[k];
-      u.x = (R)((double)u.x + c * (double)d.x);
-      u.y = (R)((double)u.y + c * (double)d.y);
+      if constexpr (SP) {
+        const float c = wh ? ar * wh[k] : ar;
+        u.x = fmaf(c, d.x, u.x);
+        u.y = fmaf(c, d.y, u.y);
+      } else {
+        const double c = wh ? a * (double)wh[k] : a;
+        u.x = (R)((double)u.x + c * (double)d.x);
+        u.y = (R)((double)u.y + c * (double)d.y);
+      }
       fh[k] = u;
     }
   double s = 0.0;
   for (long long k = k0; k < M; k += stride) {
     typename Cx<R>::T u = r[k];
     const typename Cx<R>::T d = v[k];
-    u.x = (R)((double)u.x - a * (double)d.x);
-    u.y = (R)((double)u.y - a * (double)d.y);
+    if constexpr (SP) {
+      u.x = fmaf(-ar, d.x, u.x);
+      u.y = fmaf(-ar, d.y, u.y);
+    } else {
+      u.x = (R)((double)u.x - a * (double)d.x);
+      u.y = (R)((double)u.y - a * (double)d.y);
+    }
     r[k] = u;
     const double q = (double)u.x * (double)u.x + (double)u.y * (double)u.y;
     s += w ? (double)w[k] * q : q;

@@ -100,6 +100,12 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the first sample is in (nvidia-smi
+            # takes some 0.1 s to start; a region of a few ms would otherwise
+            # end before it reports)
+            t_end = time.perf_counter() + 2.0
+            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.005)
         except Exception:
             self.proc = None
 

@@ -523,12 +523,14 @@ def run_convergence(args):
     """Where CGNR gets on the spiral trajectory of the learned workload (one
     trajectory, noiseless data, 20-ellipse phantom): for the FP64 solver, the
     FP32 solver with FP64 inner products and the same with an FP64 residual
-    refresh every 10 steps, unweighted and with the fixed-point weights, every
+    refresh every 10 steps, unweighted and with the density weights after
+    `--fp-iters` fixed-point steps, every
     10 steps the true relative data residual (FP64 transform), the relative
     image error against the phantom and the image error in the band
     |nu| <= 0.45 the samples determine; reported: the steps to a 1e-5 residual
     and the smallest errors reached within --iters steps (unweighted; half as
-    many with weights).  A third setting runs the FP64 solver with the damping
+    many with weights; the same for the weights after twenty steps, for
+    comparison).  A last setting runs the FP64 solver with the damping
     of the reference's MRI reconstruction (PRECOMPUTE_DAMP, w_hat = 1 on the
     image's inscribed disk, applications/mri/mri2d/reconstruct_data_2d.c) on
     the phantom restricted to that disk."""
@@ -549,7 +551,10 @@ def run_convergence(args):
     y = p.f.copy()
     p.finalize()
     res = infft.TrueResidual(lib, N, x, m, y)
-    wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
+    wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, args.fp_iters).cpu().numpy()
+    # twenty steps, for comparison: the iteration amplifies the sidelobes of
+    # the point-spread function, and the solver slows down
+    wfp20 = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
     out = {}
     # the damped setting solves for the phantom restricted to the image's
     # inscribed disk, from the data of that restricted phantom
@@ -563,6 +568,7 @@ def run_convergence(args):
     q.finalize()
     res_disk = infft.TrueResidual(lib, N, x, m, y_disk)
     settings = (("unweighted", None, None, args.iters), ("fixed_point_weights", wfp, None, args.iters // 2),
+                ("fixed_point_weights_20_steps", wfp20, None, args.iters // 2),
                 ("disk_damped", None, damp, args.iters))
     for wname, w, wh, total in settings:
         yy, ft, rr = (y_disk, f_true * damp, res_disk) if wh is not None else (y, f_true, res)
@@ -589,6 +595,57 @@ def run_convergence(args):
     line = {"metric": "CGNR convergence on one spiral trajectory (2-D, N=256^2, m=6, noiseless)",
             "value": out["unweighted/fp32"]["steps_to_resid_1e-5"], "unit": "steps", "n_gpus": 1,
             "higher_is_better": False, "data": "synthetic", "runs": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_dcf_steps(args):
+    """Steps of FP32 CGNR (FP64 inner products) to a 1e-5 true relative data
+    residual on held-out spirals of the learned workload (ellipse phantoms,
+    noiseless data), with the density weights after k fixed-point steps
+    w <- w/|A A^H w| from w = 1, for each k of --fp-list, and unweighted:
+    how many steps the density weights should take.  value = the k with the
+    smallest median step count."""
+    import torch
+    import nfft_gb300
+    from nfft_gb300 import dcf, infft, workloads
+    from nfft_gb300.plan import Plan
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lib = nfft_gb300.lib()
+    N, m, n = [256, 256], 6, [512, 512]
+    ks = [int(v) for v in args.fp_list.split(",")]
+    steps = {"unweighted": []}
+    for i in range(args.test):
+        x = dcf.spiral(1000 + i, 16, 8192)
+        f_true = workloads.ellipse_phantom(256, 20, seed=1000 + i)
+        p = Plan(lib, False, N, len(x), n=n, m=m, flags=infft.PLAN_FLAGS)
+        p.x[:] = x
+        p.precompute_one_psi()
+        p.f_hat[:] = f_true
+        p.trafo()
+        y = p.f.copy()
+        p.finalize()
+        r = infft.time_to_tolerance(lib, True, N, x, m, y, tol=1e-5, max_iter=args.max_iter)
+        steps["unweighted"].append(r["iters"] if r["reached"] else None)
+        for k in ks:
+            w = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, k).cpu().numpy()
+            r = infft.time_to_tolerance(lib, True, N, x, m, y, tol=1e-5, w=w, max_iter=args.max_iter)
+            steps.setdefault("fixed_point_%d" % k, []).append(r["iters"] if r["reached"] else None)
+
+    def median(v):  # a run that did not converge counts as more than the cap
+        return float(np.median([args.max_iter + 1 if s is None else s for s in v]))
+
+    med = {name: median(v) for name, v in steps.items()}
+    best = min(ks, key=lambda k: med["fixed_point_%d" % k])
+    line = {"metric": "FP32 CGNR steps to a 1e-5 relative data residual vs fixed-point steps of the density "
+            "weights (2-D spirals)", "value": best, "unit": "fixed-point steps", "n_gpus": 1,
+            "higher_is_better": False, "data": "synthetic",
+            "config": {"workload": "2-D spiral iNFFT N=256^2 n=512^2 m=6, 16 arms x 8192", "trajectories": args.test,
+                       "cap": args.max_iter, "criterion": "||y - A f|| / ||y|| < 1e-5, A in FP64, "
+                       "checked every 5 steps"},
+            "median_steps": med,
+            "not_reached": {name: int(sum(s is None for s in v)) for name, v in steps.items()},
+            "per_trajectory": steps}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -689,10 +746,11 @@ def run_learned(args):
     """Learned density-compensation weights on 2-D spirals: N = 256^2, m = 6,
     16 interleaved Archimedean arms x 8192 samples (r = t/2, angle
     2 pi (24 t + a/16) + random rotation, radius jitter 1e-4).  The MLP is
-    trained on `--train` seeded trajectories against 20 fixed-point iterations
-    w <- w/|A A^H w|; on `--test` held-out trajectories with ellipse phantoms
-    (noiseless data) FP32 CGNR (FP64 inner products) runs with the learned
-    weights, with the fixed-point weights and unweighted until the true
+    trained on `--train` seeded trajectories against the density weights after
+    `--fp-iters` steps w <- w/|A A^H w| from w = 1 (one by default: 1/|A A^H 1|);
+    on `--test` held-out trajectories with ellipse phantoms (noiseless data)
+    FP32 CGNR (FP64 inner products) runs with the learned weights, with those
+    density weights and unweighted until the true
     relative data residual ||y - A f|| / ||y|| (A the FP64 transform) falls
     below 1e-5.  value = median wall time with the learned weights, their
     inference (features + network) included; the image errors at that point
@@ -707,7 +765,7 @@ def run_learned(args):
     N, m, arms, samples = [256, 256], 6, 16, 8192
     n = [512, 512]
     t0 = time.perf_counter()
-    feats, targets = dcf.build_training_set(lib, N, m, range(args.train), arms, samples, fp_iters=20)
+    feats, targets = dcf.build_training_set(lib, N, m, range(args.train), arms, samples, fp_iters=args.fp_iters)
     t_data = time.perf_counter() - t0
     net = dcf.DensityNet(lib)
     net.fit_standardisation(feats[: min(16, len(feats))])
@@ -738,14 +796,19 @@ def run_learned(args):
         t0 = time.perf_counter()
         w = net.weights(lib, x, n).cpu().numpy()
         t_w = time.perf_counter() - t0
-        wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, 20).cpu().numpy()
-        row = {"weights_s": t_w}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        wfp = dcf.fixed_point_weights(lib, N, x.astype(np.float32), m, args.fp_iters).cpu().numpy()
+        t_fp = time.perf_counter() - t0
+        row = {"weights_s": t_w, "fixed_point_weights_s": t_fp}
         for name, ww in (("plain", None), ("learned", w), ("fixed_point", wfp)):
             r = infft.time_to_tolerance(lib, True, N, x, m, y, tol=1e-5, w=ww, max_iter=args.max_iter)
             f = r.pop("f")
             r["rel_err_vs_f_true"], r["band_err_vs_f_true"] = infft.image_errors(f, f_true)
             if name == "learned":
                 r["seconds_with_inference"] = r["seconds"] + t_w
+            if name == "fixed_point":
+                r["seconds_with_weights"] = r["seconds"] + t_fp
             row[name] = r
         rows.append(row)
     clk = clocks.stop()
@@ -758,8 +821,8 @@ def run_learned(args):
             "higher_is_better": False, "dtype": "f32 (FP64 inner products)", "data": "synthetic",
             "config": {"workload": "2-D spiral iNFFT N=256^2 n=512^2 m=6, 16 arms x 8192, MLP 8-64-64-1",
                        "train_trajectories": args.train, "test_trajectories": args.test,
-                       "epochs": args.epochs, "criterion": "||y - A f|| / ||y|| < 1e-5, A in FP64, "
-                       "checked every 5 steps"},
+                       "epochs": args.epochs, "fixed_point_steps": args.fp_iters,
+                       "criterion": "||y - A f|| / ||y|| < 1e-5, A in FP64, checked every 5 steps"},
             "clocks": clk,
             "median": {k: {"seconds": med(k, "seconds"), "iters": med(k, "iters"),
                            "rel_err_vs_f_true": med(k, "rel_err_vs_f_true"),
@@ -770,6 +833,9 @@ def run_learned(args):
             "training": {"data_s": t_data, "train_s": t_train, "loss_first": hist[0], "loss_last": hist[-1],
                          "loss_per_epoch": hist},
             "weights_inference_s_median": float(np.median([r["weights_s"] for r in rows])),
+            "fixed_point_weights_s_median": float(np.median([r["fixed_point_weights_s"] for r in rows])),
+            "speedup_fixed_point_vs_plain": med("plain", "seconds") / max(med("fixed_point", "seconds_with_weights"),
+                                                                          1e-12),
             "per_trajectory": rows}
     print(json.dumps(line), flush=True)
     return 0
@@ -783,12 +849,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uniform",
                     choices=["uniform", "clustered", "small", "radial-pair", "infft", "learned", "batched",
-                             "convergence"])
+                             "convergence", "dcf-steps"])
     ap.add_argument("--plans", type=int, default=1024, help="plans of the batched workload")
     ap.add_argument("--train", type=int, default=256, help="training trajectories (learned)")
     ap.add_argument("--test", type=int, default=32, help="held-out trajectories (learned)")
     ap.add_argument("--epochs", type=int, default=20, help="training epochs (learned)")
     ap.add_argument("--max-iter", type=int, default=3000, help="CGNR iteration cap (learned)")
+    ap.add_argument("--fp-iters", type=int, default=1,
+                    help="fixed-point steps of the density weights (learned, convergence)")
+    ap.add_argument("--fp-list", default="1,2,3,5,10,20,40,80",
+                    help="fixed-point step counts compared by the dcf-steps workload")
     ap.add_argument("--iters", type=int, default=100, help="CGNR iterations of the iNFFT workload")
     ap.add_argument("--solver", default="all", choices=["all", "fp64", "fp32", "fp32_refresh10"],
                     help="solvers of the iNFFT workload")
@@ -803,6 +873,8 @@ def main():
         return run_learned(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "dcf-steps":
+        return run_dcf_steps(args)
     if args.workload == "convergence":
         return run_convergence(args)
     wl =workload(args.workload)

@@ -148,7 +148,10 @@ int nfftf_gb_batch_set_config(void *batch, int k, int T, int tpn);
 /* Density-compensation weights for the inverse NFFT (no counterpart in the
  * reference, whose solver takes the weights w from the caller):
  *  - nfftf_gb_dcf_fixed_point: w <- w / |A A^H w| `iters` times on the
- *    plan's nodes (w_dev: M_total reals on the device, in and out);
+ *    plan's nodes (w_dev: M_total reals on the device, in and out); from
+ *    w = 1 one step gives the density estimate 1 / |A A^H 1|, which makes the
+ *    weighted CGNR converge fastest: further steps amplify the negative
+ *    sidelobes of the full-box point-spread function A A^H;
  *  - nfft_gb_dcf_features: 8 features per 2-D node (log(1 + neighbour count)
  *    within 1, 2, 4 cells of the n0 x n1 grid, 2|x|, cos/sin of the angle and
  *    of twice the angle), feat_dev = M x 8 floats;

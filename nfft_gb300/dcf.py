@@ -5,9 +5,18 @@ fixed-point weights w <- w / |A A^H w| on the GPU transforms, the per-node
 features, and the MLP's forward, gradient and Adam steps.  PyTorch tensors
 only hold device memory.
 
-Training targets are the standardised log fixed-point weights of each
-trajectory (log(w / mean w)); the network predicts them from the features.
-The weights go to the solver's `w` (PRECOMPUTE_WEIGHT) unchanged.
+Training targets are the standardised log density weights of each
+trajectory (log(w / mean w)) after FP_ITERS steps of the fixed-point
+iteration from w = 1, by default one: w = 1 / |A A^H 1|, the classic
+density estimate.  Further steps make the weights worse for the solver: the
+point-spread function of the full frequency box (A A^H) has negative
+sidelobes, and iterating against it amplifies them (measured on 16 held-out
+16-arm spirals of the learned workload, N = 256^2, m = 6: median FP32 CGNR
+steps to a 1e-5 relative data residual 67.5 after one step, 70 after three,
+92.5 after five, 297.5 after twenty, no convergence in 3000 after eighty;
+495 unweighted).
+The network predicts the targets from the features; the weights go to the
+solver's `w` (PRECOMPUTE_WEIGHT) unchanged.
 """
 import ctypes as C
 import time
@@ -18,6 +27,7 @@ from . import abi, infft, workloads
 from .plan import Plan
 
 F_IN = 8
+FP_ITERS = 1  # fixed-point steps of the density weights (see above)
 
 
 def _fn(lib, name, res, args):
@@ -62,8 +72,9 @@ def plan_for(lib, N, x, m):
     return p, n
 
 
-def fixed_point_weights(lib, N, x, m, iters=20):
-    """Fixed-point density weights of one trajectory (torch tensor, device)."""
+def fixed_point_weights(lib, N, x, m, iters=FP_ITERS):
+    """Density weights of one trajectory after `iters` fixed-point steps
+    w <- w / |A A^H w| from w = 1 (torch tensor, device)."""
     import torch
     k = Kernels(lib)
     p, _ = plan_for(lib, N, x, m)
@@ -154,8 +165,8 @@ def spiral(i, arms=16, samples=8192, jitter=1e-4, seed_base=0):
     return workloads.spiral_nodes(arms, samples, 24.0, rot, jitter, rng)
 
 
-def build_training_set(lib, N, m, ids, arms=16, samples=8192, fp_iters=20):
-    """Features (raw) and standardised log fixed-point weights per trajectory."""
+def build_training_set(lib, N, m, ids, arms=16, samples=8192, fp_iters=FP_ITERS):
+    """Features (raw) and standardised log density weights per trajectory."""
     import torch
     n = [2 * (1 << (int(v) - 1).bit_length()) for v in N]
     feats, targets = [], []

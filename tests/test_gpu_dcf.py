@@ -110,7 +110,7 @@ def test_learned_weights_speed_up_cgnr(gpulib):
     the relative data residual below 1e-5 in fewer CGNR iterations than the
     unweighted solver on a held-out spiral (noiseless data)."""
     N, m, arms, samples = [64, 64], 6, 8, 1024
-    feats, targets = dcf.build_training_set(gpulib, N, m, range(6), arms, samples, fp_iters=20)
+    feats, targets = dcf.build_training_set(gpulib, N, m, range(6), arms, samples)
     net = dcf.DensityNet(gpulib)
     net.fit_standardisation(feats)
     for f in feats:

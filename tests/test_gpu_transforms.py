@@ -329,6 +329,27 @@ def test_single_node_and_direct_fallback(gpulib):
         assert rel_l2(gfh, tfh) < 1e-9
 
 
+@pytest.mark.parametrize("single", [False, True])
+@pytest.mark.parametrize("N,m", [([16], 4), ([32, 32], 6), ([32, 32], 4), ([16, 16, 16], 4)])
+def test_zero_nodes(gpulib, single, N, m):
+    """A plan without nodes (M = 0): the reference's loops over j < M_total do
+    nothing, so trafo writes no sample and adjoint returns f_hat = 0, on
+    every call."""
+    NN = int(np.prod(N))
+    rng = np.random.default_rng(4)
+    fh = rng.uniform(-1, 1, NN) + 1j * rng.uniform(-1, 1, NN)
+    for flags in (default_guru_flags(), default_guru_flags() | abi.NFFT_SORT_NODES):
+        p = make_plan(gpulib, single, N, 0, m=m, flags=flags)
+        p.precompute_one_psi()
+        for _ in range(2):
+            p.f_hat[:] = fh
+            p.trafo()
+            assert len(p.f) == 0
+            p.adjoint()
+            assert np.array_equal(p.f_hat, np.zeros(NN))
+        p.finalize()
+
+
 def test_check_messages(gpulib):
     p = make_plan(gpulib, False, [16, 16], 10, m=4)
     p.x[:] = 0.1

@@ -1,6 +1,6 @@
 // gb_col3.cuh -- single-precision 3-D B^T (adjoint spreading) by z-column
-// segments and 3-D B (interpolation) by sub-cell units: the hot kernels of the
-// 3-D transform.
+// segments and 3-D B (interpolation) by z-column segments or by sub-cell
+// units: the hot kernels of the 3-D transform.
 //
 // Both evaluate the Kaiser-Bessel window on the fly from its per-tap
 // polynomial form (gb_window.cpp): degree-9 Horner in the node's fractional

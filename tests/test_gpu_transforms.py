@@ -570,3 +570,82 @@ def test_2d_single_random_plans_every_width(gpulib, N, n, M, m):
     fn = gpulib.nfft_gb_tma_wait_timeouts
     fn.restype = C.c_ulonglong
     assert fn() == 0
+
+
+def _sweep_cases_fp64(seed=2026):
+    """Seeded random double-precision plans, four per dimension: N_t even and
+    above m, n_t = sigma N_t with sigma in [1.5, 2.5] (odd n_t included, at
+    least 2m + 3), m in 2..8, M in 100..20000, uniform nodes; every second
+    plan sorts its nodes."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    lim = {1: (8, 129), 2: (4, 33), 3: (3, 11)}
+    for d in (1, 2, 3):
+        for k in range(4):
+            m = int(rng.integers(2, 9))
+            lo, hi = lim[d]
+            N = [int(2 * rng.integers(max(lo, m // 2 + 1), hi)) for _ in range(d)]
+            n = [max(int(np.ceil(rng.uniform(1.5, 2.5) * v)), 2 * m + 3) for v in N]
+            cases.append((N, n, int(rng.integers(100, 20001)), m, k % 2 == 1))
+    return cases
+
+
+@pytest.mark.parametrize("N,n,M,m,sort", _sweep_cases_fp64())
+def test_double_random_plans(gpulib, N, n, M, m, sort):
+    """Random double-precision plans of every dimension: trafo and adjoint
+    against the oracle to 1e-12, index_x bit for bit where the nodes are
+    sorted."""
+    x, fh, f = seeded_case(N, M, seed=M + 7)
+    flags = default_guru_flags() | (abi.NFFT_SORT_NODES if sort else 0)
+    p = make_plan(gpulib, False, N, M, m=m, n=n, flags=flags)
+    gf, gfh = run_both(p, x, fh, f)
+    idx = p.index_x if sort else None
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m, single=False)
+    o.set_nodes(x)
+    o.precompute()
+    if sort:
+        assert np.array_equal(idx, o.index_x())
+    e_t, e_a = rel_l2(gf, o.trafo(fh)), rel_l2(gfh, o.adjoint(f))
+    o.close()
+    assert e_t < 1e-12 and e_a < 1e-12, (e_t, e_a)
+
+
+def _sweep_cases_fp32_other(seed=2027):
+    """Seeded random single-precision plans off the column kernels: 1-D
+    (m in 2..8), 3-D with m in {2, 3, 5, 6} and 2-D with m = 8 (the tiled
+    kernels); N_t even, n_t = sigma N_t with sigma in [1.5, 2.5] (odd n_t
+    included), M in 100..20000."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for d, ms, lo, hi in ((1, (2, 4, 6, 8), 8, 129), (3, (2, 3, 5, 6), 3, 11), (2, (8, 8), 8, 33)):
+        for m in ms:
+            N = [int(2 * rng.integers(max(lo, m // 2 + 1), hi)) for _ in range(d)]
+            n = [max(int(np.ceil(rng.uniform(1.5, 2.5) * v)), 2 * m + 3) for v in N]
+            cases.append((N, n, int(rng.integers(100, 20001)), m))
+    return cases
+
+
+@pytest.mark.parametrize("N,n,M,m", _sweep_cases_fp32_other())
+def test_single_random_plans_tiled_paths(gpulib, N, n, M, m):
+    """Random single-precision plans on the tiled kernels: trafo and adjoint
+    against the oracle (FP64, on the single-precision inputs) to 2e-5, and
+    index_x bit for bit."""
+    x, fh, f = seeded_case(N, M, seed=M + 11)
+    x32, fh32, f32 = x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64)
+    p = make_plan(gpulib, True, N, M, m=m, n=n, flags=default_guru_flags() | abi.NFFT_SORT_NODES)
+    gf, gfh = run_both(p, x32, fh32, f32)
+    idx = p.index_x
+    p.finalize()
+    o = oracle.OraclePlan(N, M, n=n, m=m, single=True)
+    o.set_nodes(x32)
+    o.precompute()
+    assert np.array_equal(idx, o.index_x())
+    o.close()
+    od = oracle.OraclePlan(N, M, n=n, m=m, single=False)
+    od.set_nodes(x32.astype(np.float64))
+    od.precompute()
+    e_t = rel_l2(gf.astype(np.complex128), od.trafo(fh32.astype(np.complex128)))
+    e_a = rel_l2(gfh.astype(np.complex128), od.adjoint(f32.astype(np.complex128)))
+    od.close()
+    assert e_t < 2e-5 and e_a < 2e-5, (e_t, e_a)

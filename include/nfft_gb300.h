@@ -34,14 +34,13 @@ void *X(gb_get_stream)(X(plan) *ths); \
  * d != 2, NDFT). */ \
 int X(gb_set_compensated)(X(plan) *ths, int mode); \
 /* Kernel of B (trafo) for single-precision 3-D plans with m = 4: mode 0 \
- * chooses by node density at node set-up (the default: sub-cell units where \
- * the work items hold 1536 nodes or more on average, column segments \
- * otherwise), 1 column segments, 2 sub-cell units.  Both give the same \
+ * (the default) or 1 column segments, 2 sub-cell units (the column form is \
+ * as fast or faster at every node density measured).  Both give the same \
  * result to rounding.  Returns 0, or -1 (nothing changed) for a plan without \
  * these kernels. */ \
 int X(gb_set_b3_kernel)(X(plan) *ths, int mode); \
-/* The B kernel such a plan runs now (after node set-up, where mode 0 \
- * decides): 1 column segments, 2 sub-cell units; -1 for other plans. */ \
+/* The B kernel such a plan runs now: 1 column segments, 2 sub-cell units; \
+ * -1 for other plans. */ \
 int X(gb_b3_kernel)(X(plan) *ths); \
 /* Device buffers of the plan: f_hat (N_total complex), f (M_total complex), \
  * in the caller's natural orders, and x (M_total*d reals, node-major). */ \

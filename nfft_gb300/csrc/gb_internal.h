@@ -94,11 +94,6 @@ bool encode_grid_map(CUtensorMap *map, void *grid, const int *n, int ext, int ex
 // the 2-D view f32 [n_0][2 n_1] with boxes of ext rows of zb complex values
 // (zb even); false where it cannot be encoded (odd n_1)
 bool encode_grid_map_2d(CUtensorMap *map, void *grid, const int *n, int ext, int zb);
-// mean nodes per work item from which the 3-D single-precision B runs by
-// sub-cell units rather than column segments (measured on GB300: at 512 nodes
-// per item column segments take 3.79 ms against 3.97, at about 3000 sub-cell
-// units 3.47 against 3.64)
-static constexpr int B3_DENSE = 1536;
 // y extent of the 3-D column kernels' subgrid box for window width w
 int col3_box_ext_y(int w);
 // Device-side wait time-outs recorded since the last call (bounded waits on

@@ -74,8 +74,7 @@ struct Ctx {
   WinPolyD polyd = {};   // the same in double precision (2-D double-precision kernels)
   bool col2 = false;     // 2-D column kernels (nodes keyed by column)
   int comp = 0;          // compensated 2-D single-precision B^T (nfftf_gb_set_compensated), off by default
-  int b3mode = 0;        // 3-D single-precision B (nfftf_gb_set_b3_kernel): 0 by node density, 1 column segments, 2 sub-cell units
-  bool b3dense = false;  // node set-up: the work items hold B3_DENSE nodes or more on average
+  int b3mode = 0;        // 3-D single-precision B (nfftf_gb_set_b3_kernel): 0 or 1 column segments, 2 sub-cell units
   void *grid_lo = nullptr;  // its error grid (n_total complex), allocated on first use
   bool col3 = false;     // single-precision column / sub-cell kernels (node records below)
   float4 *c3rec = nullptr;
@@ -507,7 +506,6 @@ static void nodes_from_device(typename Api<R>::plan *ths, Ctx<R> *c)
       if (c->col3) launch_c3_setup(c->xs, g, c->items, c->nitems, k1, c->c3rec, c->c3cst, c->c3sst, s);
     // dense work items favour B by sub-cell units (per-unit work shared by
     // more nodes), sparse ones B by column segments
-    c->b3dense = c->nitems > 0 && (double)g.M >= (double)B3_DENSE * c->nitems;
     if (cnt != k2) {
       GB_CUDA(cudaFree(cnt));
       GB_CUDA(cudaFree(off));
@@ -563,7 +561,11 @@ static Col3Bufs col3_bufs(Ctx<R> *c)
   b.cst = c->c3cst;
   b.sst = c->c3sst;
   b.grid_map = c->grid_map_ok ? &c->grid_map : nullptr;
-  b.b_column = c->b3mode == 1 || (c->b3mode == 0 && !c->b3dense);
+  // column segments unless the sub-cell form is asked for (measured on GB300
+  // at 2^24 nodes, 128^3 / 256^3, m = 4: the column form is as fast or faster
+  // from uniform nodes (3.58 against 3.97 ms) to 32 tight clusters of spread
+  // 0.005 (3.16 against 3.20 ms))
+  b.b_column = c->b3mode != 2;
   return b;
 }
 
@@ -943,9 +945,8 @@ static int set_compensated(typename Api<R>::plan *ths, int mode)
   return 0;
 }
 
-// mode 0 (by node density, the default), 1 (column segments) or 2 (sub-cell
-// units) for the 3-D single-precision B; -1 returned where the plan runs no
-// such kernel
+// mode 0 (the default) or 1 (column segments), or 2 (sub-cell units) for the
+// 3-D single-precision B; -1 returned where the plan runs no such kernel
 template <typename R>
 static int set_b3_kernel(typename Api<R>::plan *ths, int mode)
 {

@@ -417,9 +417,8 @@ def test_3d_single_grids_with_and_without_tma_tiles(gpulib, N, n):
 def test_3d_single_b_kernels_against_oracle(gpulib, M):
     """Both kernels of the single-precision 3-D B (nfftf_gb_set_b3_kernel:
     column segments and sub-cell units) against the oracle on the same plan,
-    at sparse (94 nodes per 8^3 tile) and dense (4688) nodes; the default
-    choice follows the density (column segments below 1536 nodes per work
-    item, sub-cell units above)."""
+    at sparse (94 nodes per 8^3 tile) and dense (4688) nodes; the default is
+    the column form at any density, and mode 0 returns to it."""
     import ctypes as C
     N, n, m = [16, 16, 16], [32, 32, 32], 4
     x, fh, _ = seeded_case(N, M, seed=41)
@@ -431,7 +430,7 @@ def test_3d_single_b_kernels_against_oracle(gpulib, M):
     get.restype, get.argtypes = C.c_int, [C.c_void_p]
     setk = gpulib.nfftf_gb_set_b3_kernel
     setk.restype, setk.argtypes = C.c_int, [C.c_void_p, C.c_int]
-    assert get(pa) == (1 if M < 1536 * 64 else 2)
+    assert get(pa) == 1
     o = oracle.OraclePlan(N, M, n=n, m=m)
     o.set_nodes(x.astype(np.float32).astype(np.float64))
     o.precompute()
@@ -443,6 +442,7 @@ def test_3d_single_b_kernels_against_oracle(gpulib, M):
         p.f_hat[:] = fh.astype(np.complex64)
         p.trafo()
         got[mode] = p.f.astype(np.complex128)
+    assert setk(pa, 0) == 0 and get(pa) == 1
     p.finalize()
     e1, e2 = rel_l2(got[1], want), rel_l2(got[2], want)
     print("M=%d: column segments %.2e, sub-cell units %.2e relative l2 to the oracle" % (M, e1, e2))

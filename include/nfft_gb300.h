@@ -153,7 +153,8 @@ int nfftf_gb_batch_set_config(void *batch, int k, int T, int tpn);
  *    sidelobes of the full-box point-spread function A A^H;
  *  - nfft_gb_dcf_features: 8 features per 2-D node (log(1 + neighbour count)
  *    within 1, 2, 4 cells of the n0 x n1 grid, 2|x|, cos/sin of the angle and
- *    of twice the angle), feat_dev = M x 8 floats;
+ *    of twice the angle), feat_dev = M x 8 floats, written in stream order
+ *    (the call does not wait for them);
  *  - an MLP 8 -> 64 -> 64 -> 1 (GELU) on those features: parameter vector of
  *    nfft_gb_mlp_param_count() floats (W1[8][64], b1, W2[64][64], b2, W3, b3),
  *    forward, mean-squared-error gradient (grad and loss overwritten) and an

@@ -79,7 +79,10 @@ __global__ void __launch_bounds__(MLP_THREADS) k_mlp_forward(const float *__rest
                                                              const float *__restrict__ feat, int M,
                                                              float *__restrict__ out)
 {
-  __shared__ float P[P_COUNT];
+  // the weights in shared memory, read four outputs at a time (one 16-byte
+  // broadcast load feeds four FMAs; each output's sum keeps its order)
+  __shared__ __align__(16) float P[P_COUNT];
+  static_assert(P_W1 % 4 == 0 && P_W2 % 4 == 0 && H1 % 4 == 0 && H2 % 4 == 0, "16-byte weight rows");
   for (int i = threadIdx.x; i < P_COUNT; i += blockDim.x) P[i] = params[i];
   __syncthreads();
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
@@ -88,18 +91,36 @@ __global__ void __launch_bounds__(MLP_THREADS) k_mlp_forward(const float *__rest
     for (int i = 0; i < F_IN; ++i) xin[i] = feat[(long long)s * F_IN + i];
     float h1[H1];
 #pragma unroll
-    for (int k = 0; k < H1; ++k) {
-      float a = P[P_B1 + k];
+    for (int k = 0; k < H1; k += 4) {
+      float a0 = P[P_B1 + k], a1 = P[P_B1 + k + 1], a2 = P[P_B1 + k + 2], a3 = P[P_B1 + k + 3];
 #pragma unroll
-      for (int i = 0; i < F_IN; ++i) a += xin[i] * P[P_W1 + i * H1 + k];
-      h1[k] = gelu(a);
+      for (int i = 0; i < F_IN; ++i) {
+        const float4 w = *reinterpret_cast<const float4 *>(&P[P_W1 + i * H1 + k]);
+        a0 += xin[i] * w.x;
+        a1 += xin[i] * w.y;
+        a2 += xin[i] * w.z;
+        a3 += xin[i] * w.w;
+      }
+      h1[k] = gelu(a0);
+      h1[k + 1] = gelu(a1);
+      h1[k + 2] = gelu(a2);
+      h1[k + 3] = gelu(a3);
     }
     float o = P[P_B3];
-    for (int j = 0; j < H2; ++j) {
-      float a = P[P_B2 + j];
+    for (int j = 0; j < H2; j += 4) {
+      float a0 = P[P_B2 + j], a1 = P[P_B2 + j + 1], a2 = P[P_B2 + j + 2], a3 = P[P_B2 + j + 3];
 #pragma unroll
-      for (int k = 0; k < H1; ++k) a += h1[k] * P[P_W2 + k * H2 + j];
-      o += P[P_W3 + j] * gelu(a);
+      for (int k = 0; k < H1; ++k) {
+        const float4 w = *reinterpret_cast<const float4 *>(&P[P_W2 + k * H2 + j]);
+        a0 += h1[k] * w.x;
+        a1 += h1[k] * w.y;
+        a2 += h1[k] * w.z;
+        a3 += h1[k] * w.w;
+      }
+      o += P[P_W3 + j] * gelu(a0);
+      o += P[P_W3 + j + 1] * gelu(a1);
+      o += P[P_W3 + j + 2] * gelu(a2);
+      o += P[P_W3 + j + 3] * gelu(a3);
     }
     out[s] = o;
   }
@@ -270,15 +291,16 @@ int nfft_gb_dcf_features(const float *x_dev, int M, int n0, int n1, float *feat_
   if (M < 0 || n0 < 1 || n1 < 1) return -1;
   if (M == 0) return 0;
   cudaStream_t s = (cudaStream_t)stream;
+  // the cell counts in stream-ordered scratch: no device-wide synchronisation,
+  // the features are ready in stream order like the other entry points' results
   int *cnt = nullptr;
-  GB_CUDA(cudaMalloc(&cnt, (size_t)n0 * n1 * sizeof(int)));
+  GB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&cnt), (size_t)n0 * n1 * sizeof(int), s));
   GB_CUDA(cudaMemsetAsync(cnt, 0, (size_t)n0 * n1 * sizeof(int), s));
   k_cell_counts<<<(M + 255) / 256, 256, 0, s>>>(x_dev, M, n0, n1, cnt);
   GB_LAUNCHED("cell_counts");
   k_features<<<(M + 255) / 256, 256, 0, s>>>(x_dev, M, n0, n1, cnt, feat_dev);
   GB_LAUNCHED("features");
-  GB_CUDA(cudaStreamSynchronize(s));
-  GB_CUDA(cudaFree(cnt));
+  GB_CUDA(cudaFreeAsync(cnt, s));
   return 0;
 }
 
